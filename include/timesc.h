@@ -1,0 +1,167 @@
+/*
+ * timesc.h - C ABI of the GB300 k-Shape engine (drop-in for the Times-C
+ * `./test -d dev path k flag init_chose` path).
+ *
+ * All entry points return a tc_status (0 = success) and never exit the process.
+ * Device buffers passed in are owned by the caller and used in stream order on
+ * the given stream (NULL = the legacy default stream).  A context owns its
+ * scratch (spectra, Gram matrices, segment buffers) and reuses it across calls;
+ * one context must be driven from one host thread at a time.
+ *
+ * Reference interfaces replaced (paths inside the Times-C project):
+ *   tc_znorm            z_norm_gpu_x<T>        Code/include/normalization.cuh:150-177
+ *   tc_init_labels      idx_init / rand_init   Code/include/kshape.cuh:16-32
+ *   tc_sbd_assign       NCC_3D + get_pos_idx   Code/include/ncc.cuh:469-517, Code/include/kshape.cuh:35-96
+ *   tc_extract_shapes   extract_shape<T>       Code/include/shapeExtract.cuh:1058-1181 (+ sbd3D, SBD.cuh:69-85)
+ *   tc_kshape_run       k_shape / k_shape_tsl + the driver restart
+ *                                              Code/include/kshape.cuh:197-474, Code/test/test_kshape.cu:13-137
+ *   tc_read_file        readFile / read_unlabeled_File   Code/include/readfile.cuh:13-116
+ *   tc_write_labels     writeFile<int>         Code/include/readfile.cuh:121-129
+ *   tc_random_select    randomSelectK          Code/include/kshape.cuh:159-176
+ *   tc_k_from_labels    k from the label column  Code/test/test_kshape.cu:24-30
+ *   tc_fft_size         fft_size rule          Code/include/ncc.cuh:12-16, :473
+ */
+#ifndef TIMESC_H
+#define TIMESC_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define TC_ABI_VERSION 1
+
+typedef struct tc_ctx tc_ctx;
+typedef struct CUstream_st* tc_stream; /* the same type as cudaStream_t */
+
+typedef enum {
+    TC_OK = 0,
+    TC_ERR_ARG = 1,         /* invalid argument (sizes, pointers, alignment) */
+    TC_ERR_CUDA = 2,        /* a CUDA runtime call or a kernel launch failed */
+    TC_ERR_NOMEM = 3,       /* device or host allocation failed */
+    TC_ERR_IO = 4,          /* file could not be read/written or parsed */
+    TC_ERR_TIMEOUT = 5,     /* a bounded device wait ran out; the context stays usable */
+    TC_ERR_UNSUPPORTED = 6, /* size or mode not supported by this build */
+    TC_ERR_REJECTED = 7     /* job refused by admission control */
+} tc_status;
+
+typedef enum {
+    TC_MODE_COMPAT = 0,    /* the reference GPU build: FFT size rounded down, int-truncated gate, unit-norm centroids */
+    TC_MODE_CANONICAL = 1  /* k-Shape as published: FFT size >= 2m-1, real gate, re-z-normalised centroids */
+} tc_mode;
+
+typedef enum {
+    TC_PREC_FP32 = 0,      /* SIMT FP32 FFT correlation */
+    TC_PREC_BF16 = 1,      /* tensor-core (tcgen05) correlation, BF16 operands, FP32 accumulation */
+    TC_PREC_TF32 = 2       /* tensor-core (tcgen05) correlation, TF32 operands, FP32 accumulation */
+} tc_precision;
+
+/* ---------------------------------------------------------------- context */
+int tc_version(void);
+int tc_create(int device, tc_ctx** out);
+int tc_destroy(tc_ctx* ctx);
+/* Message of the last failed call on this context ("" if none). */
+const char* tc_last_error(const tc_ctx* ctx);
+
+/* ---------------------------------------------------------------- stages (device pointers) */
+/* FFT length the mode uses for series length m. */
+int tc_fft_size(int m, int mode);
+
+/* In place: each of n rows of length m becomes (x - mean) / std(ddof).  Rows with
+ * zero spread become zeros. */
+int tc_znorm(tc_ctx* ctx, float* d_x, int64_t n, int m, int ddof, tc_stream stream);
+
+/* Initial labels of init_chose=0: label_i = curand(XORWOW seeded with i) % k,
+ * written 0-based (the reference stores it +1). */
+int tc_init_labels(tc_ctx* ctx, int32_t* d_labels, int64_t n, int k, tc_stream stream);
+
+/* SBD assignment.  For every series (z-normalised row of d_x) and centroid: the
+ * normalised cross-correlation over all lags of the mode's FFT length; the series
+ * gets the centroid with the smallest 1 - max NCC (first centroid on ties).
+ * Outputs (any may be NULL except d_labels): d_labels (0-based), d_dist (that
+ * smallest distance), d_shift (the shift that aligns the series to its centroid:
+ * out[t] = x[t - shift]).  If d_old_labels is not NULL, *d_changed receives the
+ * number of labels that differ from it; d_dist_sum receives the FP64 sum of
+ * d_dist (both accumulated: zero them first). */
+int tc_sbd_assign(tc_ctx* ctx, const float* d_x, const float* d_centroids, int64_t n, int m, int k,
+                  int mode, int precision, int32_t* d_labels, float* d_dist, int32_t* d_shift,
+                  const int32_t* d_old_labels, int32_t* d_changed, double* d_dist_sum,
+                  tc_stream stream);
+
+/* Shape extraction: groups the rows by label (stable), aligns the members of each
+ * cluster whose centroid passes the mode's gate (using d_shift if given, else
+ * computing the shifts against d_centroids), re-z-normalises them, and replaces
+ * each non-empty cluster's centroid by the top eigenvector of Q S Q (S = the
+ * members' Gram matrix, Q = I - 11^T/m) with the reference's sign rule.
+ * cal_select = 1 takes the fully converged top eigenvector (the reference's
+ * syevd path).  Empty clusters keep their centroid.  d_counts (k, may be NULL)
+ * receives the cluster sizes and *h_sum_class (may be NULL) the number of
+ * non-empty clusters (this synchronises the stream). */
+int tc_extract_shapes(tc_ctx* ctx, const float* d_x, const int32_t* d_labels, const int32_t* d_shift,
+                      float* d_centroids, int64_t n, int m, int k, int mode, int cal_select,
+                      int precision, int32_t* d_counts, int* h_sum_class, tc_stream stream);
+
+/* ---------------------------------------------------------------- whole loop */
+typedef struct {
+    const float* h_data;          /* n*m raw values on the host (row-major), or NULL */
+    const float* d_data;          /* or the same on the device (not modified); one of the two */
+    int64_t n;
+    int m;
+    int k;
+    int mode;                     /* tc_mode */
+    int precision;                /* tc_precision */
+    int init_chose;               /* 0: random labels (curand), 1: k random raw rows as centroids */
+    uint32_t seed;                /* mt19937 seed of the init_chose=1 draw */
+    int max_iter;                 /* iteration cap; <= 0 means 20 (the reference's unlabelled cap) */
+    int restart;                  /* 1: rerun with cal_select=1 when <= k/2 clusters survive */
+    const int32_t* h_init_labels; /* optional 0-based initial labels instead of the curand draw */
+} tc_job;
+
+typedef struct {
+    int32_t* h_labels;            /* out: n labels, 0-based (host) */
+    float* h_centroids;           /* out: k*m centroids (host), may be NULL */
+    int iterations;               /* iterations of the last loop */
+    int sum_class;                /* non-empty clusters after the last extraction */
+    int restarted;                /* 1 if the cal_select=1 rerun happened */
+    double inertia;               /* mean distance of the last assignment */
+    double seconds;               /* wall time of the call */
+} tc_result;
+
+/* The reference's whole path after parsing: copy in (if h_data), z-normalise,
+ * initialise, iterate (extract/assign/converge in the reference's loop order for
+ * init_chose), apply the restart rule, copy labels/centroids out.  Synchronous. */
+int tc_kshape_run(tc_ctx* ctx, const tc_job* job, tc_result* result);
+
+/* ---------------------------------------------------------------- host I/O */
+/* Parse a text file: one series per line, values separated by commas (a line
+ * with a comma is split on commas only) or else by spaces/tabs.  labeled=1: the
+ * first token is an integer label.  *data (n*m) and *labels (n, or NULL) are
+ * malloc'ed and released with tc_free_host. */
+int tc_read_file(const char* path, int labeled, float** data, int32_t** labels, int64_t* n, int* m,
+                 char* err, int err_len);
+void tc_free_host(void* p);
+/* Writes "l0,l1,...,l(n-1)," on one line (labels as given). */
+int tc_write_labels(const char* path, const int32_t* labels, int64_t n);
+/* Writes k lines of m comma-separated values. */
+int tc_write_centroids(const char* path, const float* centroids, int k, int m);
+int tc_random_select(int64_t n, int k, uint32_t seed, int32_t* out);
+int tc_k_from_labels(const int32_t* labels, int64_t n);
+
+/* ---------------------------------------------------------------- synthetic workloads */
+typedef struct {
+    int64_t n;
+    int m;
+    int classes;          /* number of prototypes */
+    double noise;         /* noise sigma as a fraction of the prototype std */
+    double dirichlet;     /* > 0: class sizes ~ Dirichlet(alpha); 0: equal sizes */
+    uint64_t seed;
+} tc_gen_spec;
+/* Fills data (n*m) and labels (n, 0-based, may be NULL). */
+int tc_generate(const tc_gen_spec* spec, float* data, int32_t* labels);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

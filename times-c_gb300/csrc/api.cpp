@@ -1,0 +1,368 @@
+// C ABI entry points and the host side of the k-Shape loop.
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstring>
+#include <new>
+
+#include "tc_internal.h"
+
+namespace tc {
+
+// ncc.cuh:12-16 and :473: 1 << (int)ceil(my_log2(2m-1)) with my_log2 returning a
+// truncated int, i.e. the largest power of two <= 2m-1.  Canonical k-Shape pads to
+// 1 << bit_length(2m-1) (test_timesC.py:88), a power of two >= 2m-1.
+int fft_size(int m, int mode) {
+    int x = 2 * m - 1;
+    if (mode == TC_MODE_COMPAT) {
+        int lg = (int)(std::log((double)x) / std::log(2.0));
+        return 1 << lg;
+    }
+    int bl = 0;
+    while ((1 << bl) <= x) ++bl;
+    return 1 << bl;
+}
+
+void launch_gather_norm(const float*, const int32_t*, const int32_t*, const int32_t*, const uint8_t*, int64_t,
+                        int, float*, int, cudaStream_t);
+
+static void check_shape(int64_t n, int m, int k, int mode) {
+    TC_REQUIRE(n >= 0, TC_ERR_ARG, "n must be >= 0");
+    TC_REQUIRE(n <= (int64_t)INT32_MAX, TC_ERR_UNSUPPORTED, "n must fit in int32");
+    TC_REQUIRE(m >= 2 && m <= 8192, TC_ERR_UNSUPPORTED, "series length m must be in [2, 8192]");
+    TC_REQUIRE(k >= 1 && k <= 1024, TC_ERR_UNSUPPORTED, "k must be in [1, 1024]");
+    TC_REQUIRE(mode == TC_MODE_COMPAT || mode == TC_MODE_CANONICAL, TC_ERR_ARG, "unknown mode");
+    int F = fft_size(m, mode);
+    TC_REQUIRE(F >= 8 && F <= 16384, TC_ERR_UNSUPPORTED,
+               "FFT length " + std::to_string(F) + " outside [8, 16384] (series too short or too long for this mode)");
+}
+
+// One assignment against the current centroids.
+static void assign(tc_ctx* ctx, const float* x, const float* C, int64_t n, int m, int k, int mode, int precision,
+                   int32_t* labels, float* dist, int32_t* shift, const int32_t* old, int32_t* changed,
+                   double* dsum, cudaStream_t s) {
+    const int F = fft_size(m, mode);
+    AssignArgs a{};
+    a.x = x;
+    a.n = n;
+    a.m = m;
+    a.k = k;
+    a.F = F;
+    a.clamp2 = (mode == TC_MODE_COMPAT && 2 * m - 1 < 512) ? 1 : 0;  // get_pos_idx pads with 2
+    a.labels = labels;
+    a.dist = dist;
+    a.shift = shift;
+    a.old_labels = old;
+    a.changed = changed;
+    a.dist_sum = dsum;
+    if (precision == TC_PREC_FP32) {
+        float2* spec = ctx->ws.spectra.as<float2>((size_t)k * (F / 2 + 1));
+        launch_centroid_spectra(ctx, C, k, m, F, spec, s);
+        a.spec = spec;
+        launch_assign_fft(ctx, a, s);
+    } else {
+        TC_REQUIRE(tc_assign_supported(m, F, k, precision), TC_ERR_UNSUPPORTED,
+                   "tensor-core correlation does not support this shape/precision; use TC_PREC_FP32");
+        a.spec = nullptr;
+        launch_assign_tc(ctx, a, precision, s);
+        (void)C;
+    }
+}
+
+struct LoopState {
+    int iterations = 0;
+    int sum_class = 0;
+    double inertia = 0;
+};
+
+// kshape.cuh:197-324 (k_shape) and :332-474 (k_shape_tsl) on device-resident state.
+static LoopState run_loop(tc_ctx* ctx, const tc_job* job, const float* x, int k, int order_tsl, int cal_select,
+                          int cap, cudaStream_t s) {
+    Workspace& ws = ctx->ws;
+    const int64_t n = job->n;
+    const int m = job->m;
+    int32_t* labels = ws.labels.as<int32_t>(n);
+    int32_t* old = ws.old_labels.as<int32_t>(n);
+    int32_t* shift = ws.shift.as<int32_t>(n);
+    float* dist = ws.dist.as<float>(n);
+    float* C = ws.centroids.as<float>((size_t)k * m);
+    char* aux = ws.aux.as<char>(64);
+    int32_t* changed = reinterpret_cast<int32_t*>(aux);
+    double* dsum = reinterpret_cast<double*>(aux + 8);
+
+    // initial labels: idx_init (curand) or the caller's
+    if (job->h_init_labels)
+        TC_CUDA(cudaMemcpyAsync(labels, job->h_init_labels, sizeof(int32_t) * n, cudaMemcpyHostToDevice, s));
+    else
+        launch_init_labels(labels, n, k, s);
+    TC_CUDA(cudaMemcpyAsync(old, labels, sizeof(int32_t) * n, cudaMemcpyDeviceToDevice, s));
+    TC_CUDA(cudaMemsetAsync(C, 0, sizeof(float) * k * m, s));
+    if (order_tsl) {
+        // k distinct raw rows (kshape.cuh:159-191, :345-352), before normalisation
+        std::vector<int32_t> pick(k);
+        TC_REQUIRE(tc_random_select(n, k, job->seed, pick.data()) == TC_OK, TC_ERR_ARG, "k > n");
+        for (int j = 0; j < k; ++j) {
+            if (job->h_data)
+                TC_CUDA(cudaMemcpyAsync(C + (size_t)j * m, job->h_data + (size_t)pick[j] * m, sizeof(float) * m,
+                                        cudaMemcpyHostToDevice, s));
+            else
+                TC_CUDA(cudaMemcpyAsync(C + (size_t)j * m, job->d_data + (size_t)pick[j] * m, sizeof(float) * m,
+                                        cudaMemcpyDeviceToDevice, s));
+        }
+    }
+    LoopState st;
+    st.sum_class = k;
+    st.iterations = cap;
+    double old_inertia = 1e10;
+    int countIter = 0;
+    struct {
+        int32_t changed;
+        int32_t pad;
+        double dsum;
+    } h;
+    auto do_assign = [&]() -> bool {
+        TC_CUDA(cudaMemsetAsync(aux, 0, 16, s));
+        assign(ctx, x, C, n, m, k, job->mode, job->precision, labels, dist, shift, old, changed, dsum, s);
+        TC_CUDA(cudaMemcpyAsync(&h, aux, 16, cudaMemcpyDeviceToHost, s));
+        TC_CUDA(cudaStreamSynchronize(s));
+        st.inertia = h.dsum / (double)n;
+        return h.changed == 0;
+    };
+    auto converge = [&](int i, bool flag) -> bool {
+        if (flag || countIter > 20) {
+            st.iterations = i + 1;
+            return true;
+        }
+        if (st.inertia < old_inertia || std::fabs(old_inertia - st.inertia) < 1e-6) {
+            TC_CUDA(cudaMemcpyAsync(old, labels, sizeof(int32_t) * n, cudaMemcpyDeviceToDevice, s));
+            old_inertia = st.inertia;
+            countIter = 0;
+        } else {
+            ++countIter;
+        }
+        return false;
+    };
+    auto extract = [&]() {
+        ExtractArgs e{};
+        e.x = x;
+        e.labels = labels;
+        e.shift = shift;
+        e.C = C;
+        e.n = n;
+        e.m = m;
+        e.k = k;
+        e.mode = job->mode;
+        e.cal_select = cal_select;
+        e.precision = job->precision;
+        e.counts = nullptr;
+        int sc = run_extract(ctx, e, s);
+        if (!cal_select) st.sum_class = sc;  // get_class_centers_a leaves sum_class alone
+    };
+    bool first_extract = true;
+    for (int i = 0; i < cap; ++i) {
+        if (!order_tsl) {
+            // at i = 0 the centroids are zero, so no gate opens and no shift is read
+            if (first_extract) TC_CUDA(cudaMemsetAsync(shift, 0, sizeof(int32_t) * n, s));
+            first_extract = false;
+            extract();
+            if (st.sum_class == 1 || st.sum_class <= k / 2) {
+                st.iterations = i + 1;
+                break;
+            }
+            if (converge(i, do_assign())) break;
+        } else {
+            if (converge(i, do_assign())) break;
+            extract();
+            if (st.sum_class == 1 || st.sum_class <= k / 2) {
+                st.iterations = i + 1;
+                break;
+            }
+        }
+    }
+    return st;
+}
+
+}  // namespace tc
+
+using namespace tc;
+
+#define TC_API_BEGIN try {
+#define TC_API_END(ctx)                                           \
+    }                                                             \
+    catch (const TcError& e) {                                    \
+        if (ctx) (ctx)->last_error = e.msg;                       \
+        return e.code;                                            \
+    }                                                             \
+    catch (const std::bad_alloc&) {                               \
+        if (ctx) (ctx)->last_error = "host allocation failed";    \
+        return TC_ERR_NOMEM;                                      \
+    }                                                             \
+    catch (const std::exception& e) {                             \
+        if (ctx) (ctx)->last_error = e.what();                    \
+        return TC_ERR_ARG;                                        \
+    }                                                             \
+    return TC_OK;
+
+extern "C" {
+
+int tc_version(void) { return TC_ABI_VERSION; }
+
+int tc_create(int device, tc_ctx** out) {
+    if (!out) return TC_ERR_ARG;
+    *out = nullptr;
+    int count = 0;
+    if (cudaGetDeviceCount(&count) != cudaSuccess || device < 0 || device >= count) {
+        cudaGetLastError();
+        return TC_ERR_CUDA;
+    }
+    if (cudaSetDevice(device) != cudaSuccess) return TC_ERR_CUDA;
+    tc_ctx* c = new (std::nothrow) tc_ctx();
+    if (!c) return TC_ERR_NOMEM;
+    c->device = device;
+    cudaDeviceGetAttribute(&c->sm_count, cudaDevAttrMultiProcessorCount, device);
+    int optin = 0;
+    cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, device);
+    c->smem_optin = (size_t)optin;
+    if (cudaStreamCreateWithFlags(&c->own_stream, cudaStreamNonBlocking) != cudaSuccess) {
+        delete c;
+        return TC_ERR_CUDA;
+    }
+    *out = c;
+    return TC_OK;
+}
+
+int tc_destroy(tc_ctx* ctx) {
+    if (!ctx) return TC_ERR_ARG;
+    cudaSetDevice(ctx->device);
+    cudaStreamSynchronize(ctx->own_stream);
+    DevBuf* bufs[] = {&ctx->ws.x, &ctx->ws.labels, &ctx->ws.old_labels, &ctx->ws.shift, &ctx->ws.dist,
+                      &ctx->ws.centroids, &ctx->ws.spectra, &ctx->ws.seg, &ctx->ws.perm, &ctx->ws.chunk_counts,
+                      &ctx->ws.counts, &ctx->ws.offsets, &ctx->ws.gate, &ctx->ws.scal, &ctx->ws.gram,
+                      &ctx->ws.rowsum, &ctx->ws.piter, &ctx->ws.pstats, &ctx->ws.aux, &ctx->ws.toeplitz,
+                      &ctx->ws.xbf};
+    for (DevBuf* b : bufs) b->release();
+    for (auto* t : ctx->fft) {
+        t->twN.release();
+        t->twF.release();
+        delete t;
+    }
+    cudaStreamDestroy(ctx->own_stream);
+    delete ctx;
+    return TC_OK;
+}
+
+const char* tc_last_error(const tc_ctx* ctx) { return ctx ? ctx->last_error.c_str() : "null context"; }
+
+int tc_fft_size(int m, int mode) {
+    if (m < 1) return 0;
+    return fft_size(m, mode);
+}
+
+int tc_znorm(tc_ctx* ctx, float* d_x, int64_t n, int m, int ddof, tc_stream stream) {
+    if (!ctx) return TC_ERR_ARG;
+    TC_API_BEGIN
+    TC_REQUIRE(d_x || n == 0, TC_ERR_ARG, "null data");
+    TC_REQUIRE(ddof >= 0 && ddof < m, TC_ERR_ARG, "ddof must be in [0, m)");
+    TC_CUDA(cudaSetDevice(ctx->device));
+    launch_znorm(d_x, n, m, ddof, ctx->sm_count, (cudaStream_t)stream);
+    TC_API_END(ctx)
+}
+
+int tc_init_labels(tc_ctx* ctx, int32_t* d_labels, int64_t n, int k, tc_stream stream) {
+    if (!ctx) return TC_ERR_ARG;
+    TC_API_BEGIN
+    TC_REQUIRE(d_labels || n == 0, TC_ERR_ARG, "null labels");
+    TC_REQUIRE(k >= 1, TC_ERR_ARG, "k must be >= 1");
+    TC_CUDA(cudaSetDevice(ctx->device));
+    launch_init_labels(d_labels, n, k, (cudaStream_t)stream);
+    TC_API_END(ctx)
+}
+
+int tc_sbd_assign(tc_ctx* ctx, const float* d_x, const float* d_centroids, int64_t n, int m, int k, int mode,
+                  int precision, int32_t* d_labels, float* d_dist, int32_t* d_shift, const int32_t* d_old_labels,
+                  int32_t* d_changed, double* d_dist_sum, tc_stream stream) {
+    if (!ctx) return TC_ERR_ARG;
+    TC_API_BEGIN
+    check_shape(n, m, k, mode);
+    TC_REQUIRE((d_x && d_centroids && d_labels) || n == 0, TC_ERR_ARG, "null pointer");
+    TC_REQUIRE(precision >= TC_PREC_FP32 && precision <= TC_PREC_TF32, TC_ERR_ARG, "unknown precision");
+    TC_CUDA(cudaSetDevice(ctx->device));
+    assign(ctx, d_x, d_centroids, n, m, k, mode, precision, d_labels, d_dist, d_shift, d_old_labels, d_changed,
+           d_dist_sum, (cudaStream_t)stream);
+    TC_API_END(ctx)
+}
+
+int tc_extract_shapes(tc_ctx* ctx, const float* d_x, const int32_t* d_labels, const int32_t* d_shift,
+                      float* d_centroids, int64_t n, int m, int k, int mode, int cal_select, int precision,
+                      int32_t* d_counts, int* h_sum_class, tc_stream stream) {
+    if (!ctx) return TC_ERR_ARG;
+    TC_API_BEGIN
+    check_shape(n, m, k, mode);
+    TC_REQUIRE((d_x && d_labels) || n == 0, TC_ERR_ARG, "null pointer");
+    TC_REQUIRE(d_centroids, TC_ERR_ARG, "null centroids");
+    TC_CUDA(cudaSetDevice(ctx->device));
+    ExtractArgs e{};
+    e.x = d_x;
+    e.labels = d_labels;
+    e.shift = d_shift;
+    e.C = d_centroids;
+    e.n = n;
+    e.m = m;
+    e.k = k;
+    e.mode = mode;
+    e.cal_select = cal_select ? 1 : 0;
+    e.precision = precision;
+    e.counts = d_counts;
+    int sc = run_extract(ctx, e, (cudaStream_t)stream);
+    if (h_sum_class) *h_sum_class = sc;
+    TC_API_END(ctx)
+}
+
+int tc_kshape_run(tc_ctx* ctx, const tc_job* job, tc_result* res) {
+    if (!ctx) return TC_ERR_ARG;
+    TC_API_BEGIN
+    auto t0 = std::chrono::steady_clock::now();
+    TC_REQUIRE(job && res, TC_ERR_ARG, "null job/result");
+    TC_REQUIRE(job->n >= 1, TC_ERR_ARG, "n must be >= 1");
+    check_shape(job->n, job->m, job->k, job->mode);
+    TC_REQUIRE((job->h_data != nullptr) != (job->d_data != nullptr), TC_ERR_ARG, "give exactly one of h_data/d_data");
+    TC_REQUIRE(job->init_chose == 0 || job->init_chose == 1, TC_ERR_ARG, "init_chose must be 0 or 1");
+    TC_REQUIRE(job->init_chose == 0 || job->k <= job->n, TC_ERR_ARG, "init_chose=1 needs k <= n");
+    TC_REQUIRE(job->precision >= TC_PREC_FP32 && job->precision <= TC_PREC_TF32, TC_ERR_ARG, "unknown precision");
+    TC_REQUIRE(res->h_labels, TC_ERR_ARG, "null label output");
+    if (job->h_init_labels)
+        for (int64_t i = 0; i < job->n; ++i)
+            TC_REQUIRE(job->h_init_labels[i] >= 0 && job->h_init_labels[i] < job->k, TC_ERR_ARG,
+                       "initial label out of range");
+    TC_CUDA(cudaSetDevice(ctx->device));
+    cudaStream_t s = ctx->own_stream;
+    const int64_t n = job->n;
+    const int m = job->m, k = job->k;
+    float* x = ctx->ws.x.as<float>((size_t)n * m);
+    if (job->h_data)
+        TC_CUDA(cudaMemcpyAsync(x, job->h_data, sizeof(float) * n * m, cudaMemcpyHostToDevice, s));
+    else
+        TC_CUDA(cudaMemcpyAsync(x, job->d_data, sizeof(float) * n * m, cudaMemcpyDeviceToDevice, s));
+    launch_znorm(x, n, m, 1, ctx->sm_count, s);  // test_kshape.cu:37 / :99
+    const int cap = job->max_iter > 0 ? job->max_iter : 20;
+    LoopState st = run_loop(ctx, job, x, k, job->init_chose == 1, 0, cap, s);
+    res->restarted = 0;
+    // test_kshape.cu:54-59 / :112-117: too few clusters survived -> rerun k_shape
+    // from the random-label start with the full eigensolver.
+    if (job->restart && (st.sum_class == 1 || st.sum_class < k / 2)) {
+        res->restarted = 1;
+        st = run_loop(ctx, job, x, k, 0, 1, cap, s);
+    }
+    TC_CUDA(cudaMemcpyAsync(res->h_labels, ctx->ws.labels.p, sizeof(int32_t) * n, cudaMemcpyDeviceToHost, s));
+    if (res->h_centroids)
+        TC_CUDA(cudaMemcpyAsync(res->h_centroids, ctx->ws.centroids.p, sizeof(float) * k * m, cudaMemcpyDeviceToHost,
+                                s));
+    TC_CUDA(cudaStreamSynchronize(s));
+    res->iterations = st.iterations;
+    res->sum_class = st.sum_class;
+    res->inertia = st.inertia;
+    res->seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    TC_API_END(ctx)
+}
+
+}  // extern "C"

@@ -1,0 +1,376 @@
+// Fused SBD assignment on SIMT FP32 (the "plain FP32" form).
+//
+// Replaces NCC_3D + get_pos_idx (ncc.cuh:469-517, kshape.cuh:35-96).  The
+// reference materialises n*k*F complex products and n*k*(2m-1) correlations in
+// HBM; here one team of threads per series keeps the series spectrum in
+// registers, multiplies it by each centroid spectrum (resident in shared memory
+// when they fit), runs the inverse transform in registers + shared memory and
+// reduces the max NCC over the valid lags on the fly.  Only (label, distance,
+// shift) per series reach HBM.
+#include <curand_kernel.h>
+
+#include <cmath>
+#include <mutex>
+
+#include "sbd_core.cuh"
+#include "tc_internal.h"
+
+using namespace tcfft;
+
+namespace tc {
+
+// ------------------------------------------------------------------ tables
+const FftTables& fft_tables(tc_ctx* ctx, int F) {
+    for (auto* t : ctx->fft)
+        if (t->F == F) return *t;
+    auto* t = new FftTables();
+    t->F = F;
+    int N = F / 2;
+    std::vector<float2> hN(N), hF(N);
+    for (int e = 0; e < N; ++e) {
+        double a = -2.0 * M_PI * (double)e / (double)N;
+        double b = -2.0 * M_PI * (double)e / (double)F;
+        hN[e] = make_float2((float)std::cos(a), (float)std::sin(a));
+        hF[e] = make_float2((float)std::cos(b), (float)std::sin(b));
+    }
+    float2* dN = t->twN.as<float2>(N);
+    float2* dF = t->twF.as<float2>(N);
+    TC_CUDA(cudaMemcpy(dN, hN.data(), sizeof(float2) * N, cudaMemcpyHostToDevice));
+    TC_CUDA(cudaMemcpy(dF, hF.data(), sizeof(float2) * N, cudaMemcpyHostToDevice));
+    ctx->fft.push_back(t);
+    return *t;
+}
+
+// ------------------------------------------------------------------ team primitives
+// Lanes of the calling thread's team inside its warp (all lanes for T >= 32).
+template <int T>
+__device__ __forceinline__ unsigned team_mask() {
+    if constexpr (T >= 32) return 0xffffffffu;
+    else return ((1u << T) - 1u) << ((threadIdx.x & 31) & ~(T - 1));
+}
+
+template <int T>
+__device__ __forceinline__ void team_sync(int team) {
+    if constexpr (T <= 32) {
+        __syncwarp(team_mask<T>());
+    } else {
+        asm volatile("bar.sync %0, %1;" ::"r"(team + 1), "r"(T) : "memory");
+    }
+}
+
+struct TeamScratch {
+    double sum[16];
+    float val[16];
+    int u[16];
+};
+
+// Sum over the team; every thread gets the result.
+template <int T>
+__device__ __forceinline__ double team_sum(double v, int team, int tid, TeamScratch* scr) {
+    constexpr int W = T < 32 ? T : 32;
+#pragma unroll
+    for (int o = W / 2; o > 0; o >>= 1) v += __shfl_xor_sync(team_mask<T>(), v, o, W);
+    if constexpr (T > 32) {
+        if ((tid & 31) == 0) scr->sum[tid >> 5] = v;
+        team_sync<T>(team);
+        v = 0;
+#pragma unroll
+        for (int w = 0; w < T / 32; ++w) v += scr->sum[w];
+        team_sync<T>(team);
+    }
+    return v;
+}
+
+// (val, u) max over the team (larger u wins ties); valid on tid 0.
+template <int T>
+__device__ __forceinline__ LagMax team_max(LagMax lm, int team, int tid, TeamScratch* scr) {
+    constexpr int W = T < 32 ? T : 32;
+#pragma unroll
+    for (int o = W / 2; o > 0; o >>= 1) {
+        float ov = __shfl_xor_sync(team_mask<T>(), lm.val, o, W);
+        int ou = __shfl_xor_sync(team_mask<T>(), lm.u, o, W);
+        lm.take(ov, ou);
+    }
+    if constexpr (T > 32) {
+        if ((tid & 31) == 0) {
+            scr->val[tid >> 5] = lm.val;
+            scr->u[tid >> 5] = lm.u;
+        }
+        team_sync<T>(team);
+        if (tid == 0)
+            for (int w = 1; w < T / 32; ++w) lm.take(scr->val[w], scr->u[w]);
+    }
+    return lm;
+}
+
+// Stockham passes PS..NPASS-1 over the team buffer.
+template <int N, int PS, bool INV, bool STORE_LAST, class Out>
+__device__ __forceinline__ void run_passes(float2* buf, int tid, int team, const float2* __restrict__ twN, Out& out) {
+    typedef Core<N> C;
+    typename C::template Pass<PS> st;
+    st.load(buf, tid);
+    constexpr bool last = PS + 1 >= Plan<N>::NPASS;
+    if constexpr (!last || STORE_LAST) {
+        team_sync<C::T>(team);
+        st.template compute<INV>(tid, twN);
+        st.store(buf, tid);
+        team_sync<C::T>(team);
+    } else {
+        st.template compute<INV>(tid, twN);
+        st.each_output(tid, out);
+    }
+    if constexpr (!last) run_passes<N, PS + 1, INV, STORE_LAST>(buf, tid, team, twN, out);
+}
+
+struct NoOut {
+    __device__ void operator()(int, float2) const {}
+};
+
+// Forward transform of one row into the thread's spectrum registers.
+template <int N>
+__device__ __forceinline__ void forward_row(const float* __restrict__ x, int m, float2* buf, int tid, int team,
+                                            const float2* __restrict__ twN, const float2* __restrict__ twF,
+                                            TeamScratch* scr, double extra, float2 (&xh)[2][Plan<N>::R0],
+                                            float& xhN, double& nrm2) {
+    typedef Core<N> C;
+    float2 v[2][C::R0];
+    float ss = C::fwd_load(x, m, tid, v);
+    nrm2 = team_sum<C::T>((double)ss, team, tid, scr);
+    C::template pass0_store<false>(v, tid, buf);
+    team_sync<C::T>(team);
+    NoOut no;
+    run_passes<N, 1, false, true>(buf, tid, team, twN, no);
+    float s = nrm2 > 0 ? (float)(1.0 / (std::sqrt(nrm2) * extra)) : 0.f;
+    C::post(buf, tid, twF, s, xh, xhN);
+    team_sync<C::T>(team);
+}
+
+template <int N>
+struct Cfg {
+    static constexpr int T = Plan<N>::T;
+    static constexpr int BLOCK = T > 512 ? T : 512;
+    static constexpr int TEAMS = BLOCK / T;
+    static constexpr size_t BUF_BYTES = (size_t)BufSize<N>::value * sizeof(float2);
+    static size_t smem(int k, bool csmem) {
+        size_t s = (size_t)TEAMS * (BUF_BYTES + sizeof(TeamScratch));
+        if (csmem) s += ((size_t)k * (N + 1) * sizeof(float2) + 15) / 16 * 16;  // as laid out in the kernel
+        return s;
+    }
+};
+
+// ------------------------------------------------------------------ centroid spectra
+template <int N>
+__global__ void __launch_bounds__(Plan<N>::T) k_centroid_spectra(const float* __restrict__ C, int m,
+                                                                 const float2* __restrict__ twN,
+                                                                 const float2* __restrict__ twF,
+                                                                 float2* __restrict__ spec) {
+    typedef Core<N> Co;
+    extern __shared__ __align__(16) unsigned char smem[];
+    float2* buf = reinterpret_cast<float2*>(smem);
+    TeamScratch* scr = reinterpret_cast<TeamScratch*>(smem + Cfg<N>::BUF_BYTES);
+    const int tid = threadIdx.x, j = blockIdx.x;
+    float2 xh[2][Co::R0];
+    float xhN = 0.f;
+    double nrm2;
+    forward_row<N>(C + (size_t)j * m, m, buf, tid, 0, twN, twF, scr, 2.0 * N, xh, xhN, nrm2);
+    float2* S = spec + (size_t)j * (N + 1);
+#pragma unroll
+    for (int b = 0; b < 2; ++b)
+#pragma unroll
+        for (int r = 0; r < Co::R0; ++r) S[Co::j_of(tid, b) + r * Co::NB0] = xh[b][r];
+    if (tid == 0) S[N] = make_float2(xhN, 0.f);
+}
+
+// ------------------------------------------------------------------ assignment
+struct AssignParams {
+    const float* x;
+    const float2* spec;
+    const float2* twN;
+    const float2* twF;
+    int64_t n;
+    int m, k, F, clamp2;
+    const int32_t* fixed;
+    int32_t* labels;
+    float* dist;
+    int32_t* shift;
+    const int32_t* old_labels;
+    int32_t* changed;
+    double* dist_sum;
+};
+
+struct LagOut {
+    LagMax lm;
+    int m, F;
+    __device__ void operator()(int o, float2 v) {
+        lag_take(lm, 2 * o, v.x, m, F);
+        lag_take(lm, 2 * o + 1, v.y, m, F);
+    }
+};
+
+template <int N, bool CSMEM>
+__global__ void __launch_bounds__(Cfg<N>::BLOCK, 1) k_assign_fft(AssignParams p) {
+    typedef Core<N> Co;
+    constexpr int T = Co::T, TEAMS = Cfg<N>::TEAMS;
+    extern __shared__ __align__(16) unsigned char smem[];
+    unsigned char* cur = smem;
+    float2* cspec = reinterpret_cast<float2*>(cur);
+    if (CSMEM) cur += ((size_t)p.k * (N + 1) * sizeof(float2) + 15) / 16 * 16;
+    const int team = threadIdx.x / T, tid = threadIdx.x % T;
+    float2* buf = reinterpret_cast<float2*>(cur) + (size_t)team * BufSize<N>::value;
+    TeamScratch* scr = reinterpret_cast<TeamScratch*>(cur + (size_t)TEAMS * Cfg<N>::BUF_BYTES) + team;
+
+    if (CSMEM) {
+        const size_t nv = (size_t)p.k * (N + 1);
+        for (size_t e = threadIdx.x; e < nv; e += blockDim.x) cspec[e] = p.spec[e];
+        __syncthreads();
+    }
+
+    double dsum = 0.0;
+    int nchg = 0;
+    const int64_t stride = (int64_t)gridDim.x * TEAMS;
+    for (int64_t i = (int64_t)blockIdx.x * TEAMS + team; i < p.n; i += stride) {
+        float2 xh[2][Co::R0];
+        float xhN = 0.f;
+        double nrm2;
+        forward_row<N>(p.x + (size_t)i * p.m, p.m, buf, tid, team, p.twN, p.twF, scr, 1.0, xh, xhN, nrm2);
+        int c0 = 0, c1 = p.k;
+        if (p.fixed) {
+            c0 = p.fixed[i];
+            c1 = c0 + 1;
+        }
+        float bestd = 1e10f;  // get_pos_idx: min_val = 1e10, pos = 0
+        int bestj = 0, bests = 0;
+        for (int c = c0; c < c1; ++c) {
+            float2 v[2][Co::R0];
+            if (CSMEM) {
+                const float2* S = cspec + (size_t)c * (N + 1);
+                Co::product(xh, xhN, [S](int f) { return S[f]; }, tid, p.twF, v);
+            } else {
+                const float2* S = p.spec + (size_t)c * (N + 1);
+                Co::product(xh, xhN, [S](int f) { return __ldg(S + f); }, tid, p.twF, v);
+            }
+            Co::template pass0_store<true>(v, tid, buf);
+            team_sync<T>(team);
+            LagOut out;
+            out.lm.init();
+            out.m = p.m;
+            out.F = p.F;
+            run_passes<N, 1, true, false>(buf, tid, team, p.twN, out);
+            LagMax lm = team_max<T>(out.lm, team, tid, scr);
+            team_sync<T>(team);
+            if (tid == 0) {
+                float d = 1.0f - lm.val;
+                if (p.clamp2 && d > 2.0f) d = 2.0f;
+                if (d < bestd) {
+                    bestd = d;
+                    bestj = c;
+                    bests = -lm.u;
+                }
+            }
+        }
+        if (tid == 0) {
+            if (p.labels) p.labels[i] = bestj;
+            if (p.dist) p.dist[i] = bestd;
+            if (p.shift) p.shift[i] = bests;
+            dsum += (double)bestd;
+            if (p.old_labels && p.old_labels[i] != bestj) ++nchg;
+        }
+    }
+    if (tid == 0) {
+        if (p.dist_sum) atomicAdd(p.dist_sum, dsum);
+        if (p.changed && nchg) atomicAdd(p.changed, nchg);
+    }
+}
+
+// ------------------------------------------------------------------ dispatch
+template <int N>
+static void centroid_spectra_n(tc_ctx* ctx, const float* C, int k, int m, float2* spec, cudaStream_t s) {
+    const FftTables& tb = fft_tables(ctx, 2 * N);
+    size_t sm = Cfg<N>::BUF_BYTES + sizeof(TeamScratch);
+    TC_CUDA(cudaFuncSetAttribute(k_centroid_spectra<N>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+    k_centroid_spectra<N><<<k, Plan<N>::T, sm, s>>>(C, m, (const float2*)tb.twN.p, (const float2*)tb.twF.p, spec);
+    TC_CHECK_LAUNCH();
+}
+
+template <int N>
+static void assign_n(tc_ctx* ctx, const AssignArgs& a, cudaStream_t s) {
+    const FftTables& tb = fft_tables(ctx, 2 * N);
+    AssignParams p;
+    p.x = a.x;
+    p.spec = a.spec;
+    p.twN = (const float2*)tb.twN.p;
+    p.twF = (const float2*)tb.twF.p;
+    p.n = a.n;
+    p.m = a.m;
+    p.k = a.k;
+    p.F = a.F;
+    p.clamp2 = a.clamp2;
+    p.fixed = a.fixed;
+    p.labels = a.labels;
+    p.dist = a.dist;
+    p.shift = a.shift;
+    p.old_labels = a.old_labels;
+    p.changed = a.changed;
+    p.dist_sum = a.dist_sum;
+    bool csmem = Cfg<N>::smem(a.k, true) <= ctx->smem_optin;
+    size_t sm = Cfg<N>::smem(a.k, csmem);
+    int64_t teams_needed = (a.n + Cfg<N>::TEAMS - 1) / Cfg<N>::TEAMS;
+    int grid;
+    if (csmem) {
+        TC_CUDA(cudaFuncSetAttribute(k_assign_fft<N, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+        int per_sm = 0;
+        TC_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_assign_fft<N, true>, Cfg<N>::BLOCK, sm));
+        grid = (int)std::min<int64_t>(teams_needed, (int64_t)ctx->sm_count * std::max(per_sm, 1));
+        k_assign_fft<N, true><<<grid, Cfg<N>::BLOCK, sm, s>>>(p);
+    } else {
+        TC_CUDA(cudaFuncSetAttribute(k_assign_fft<N, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+        int per_sm = 0;
+        TC_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_assign_fft<N, false>, Cfg<N>::BLOCK, sm));
+        grid = (int)std::min<int64_t>(teams_needed, (int64_t)ctx->sm_count * std::max(per_sm, 1));
+        k_assign_fft<N, false><<<grid, Cfg<N>::BLOCK, sm, s>>>(p);
+    }
+    TC_CHECK_LAUNCH();
+}
+
+#define TC_FOR_EACH_N(X) X(4) X(8) X(16) X(32) X(64) X(128) X(256) X(512) X(1024) X(2048) X(4096) X(8192)
+
+void launch_centroid_spectra(tc_ctx* ctx, const float* C, int k, int m, int F, float2* spec, cudaStream_t s) {
+    switch (F / 2) {
+#define X(n) \
+    case n: centroid_spectra_n<n>(ctx, C, k, m, spec, s); return;
+        TC_FOR_EACH_N(X)
+#undef X
+    }
+    throw TcError{TC_ERR_UNSUPPORTED, "FFT length " + std::to_string(F) + " not supported (8..16384)"};
+}
+
+void launch_assign_fft(tc_ctx* ctx, const AssignArgs& a, cudaStream_t s) {
+    if (a.n == 0) return;
+    switch (a.F / 2) {
+#define X(n) \
+    case n: assign_n<n>(ctx, a, s); return;
+        TC_FOR_EACH_N(X)
+#undef X
+    }
+    throw TcError{TC_ERR_UNSUPPORTED, "FFT length " + std::to_string(a.F) + " not supported (8..16384)"};
+}
+
+// ------------------------------------------------------------------ curand label init
+// kshape.cuh:16-32: curand_init(seed = series index, subsequence 0, offset 0),
+// label = curand() % k (+1 in the reference; stored 0-based here).
+__global__ void k_init_labels(int32_t* labels, int64_t n, int k) {
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) {
+        curandState_t st;
+        curand_init((unsigned int)i, 0, 0, &st);
+        labels[i] = (int32_t)(curand(&st) % (unsigned int)k);
+    }
+}
+
+void launch_init_labels(int32_t* labels, int64_t n, int k, cudaStream_t s) {
+    if (n == 0) return;
+    k_init_labels<<<ceil_div(n, 256), 256, 0, s>>>(labels, n, k);
+    TC_CHECK_LAUNCH();
+}
+
+}  // namespace tc

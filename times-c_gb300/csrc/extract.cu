@@ -1,0 +1,537 @@
+// Shape extraction (extract_shape, shapeExtract.cuh:1058-1181).
+//
+//   segment   stable counting sort of series by label: chunk histograms, a scan
+//             per cluster over chunks, a scan over clusters, and a stable scatter
+//             (warp match + per-warp counts) - replaces class_count/get_loc2
+//             (a single-thread loop for n < 1e6) and block_alloc2D (:21-188).
+//   gate      per-cluster alignment gate (:1129-1135).
+//   gather    align + re-z-normalise members into cluster order (znorm.cu).
+//   Gram      S_c = sum_{i in c} y_i y_i^T (:532-537), SIMT FP32 here; the
+//             tensor-core version lives in gram_tc.cu.
+//   centring  M = Q S Q is never formed: M v = S v - (1.v/m) r - (r.v/m) 1
+//             + (tot 1.v/m^2) 1 with r = S 1, tot = 1^T S 1 (replaces get_matQ and
+//             two in-place m^3 GEMMs, :204-214, :551-570).
+//   power     all clusters advance together, one launch per step, with the
+//             Rayleigh quotient, the step difference and the norms in FP64
+//             (:269-360, :577-630); the sign rule and the store are fused into
+//             the final kernel (get_center, :217-264).
+#include <algorithm>
+#include <cmath>
+
+#include "tc_internal.h"
+
+namespace tc {
+
+void launch_gather_norm(const float* x, const int32_t* perm, const int32_t* labels, const int32_t* shift,
+                        const uint8_t* gate, int64_t n, int m, float* seg, int sm_count, cudaStream_t s);
+bool gram_tc_supported(int m, int precision);
+void launch_gram_tc(tc_ctx* ctx, const float* seg, const int32_t* counts, const int32_t* offsets, int k, int m,
+                    int precision, float* S, cudaStream_t s);
+
+constexpr int SEG_CHUNK = 4096;
+constexpr int SEG_BLOCK = 256;
+constexpr int MAX_K = 1024;
+
+__device__ __forceinline__ double block_sum_d(double v, double* red) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    __syncthreads();
+    if (lane == 0) red[wid] = v;
+    __syncthreads();
+    double s = 0;
+    for (int w = 0; w < nw; ++w) s += red[w];
+    return s;
+}
+
+// ---------------------------------------------------------------- segment
+// Labels outside [0, k) are not counted; they raise *bad, which the host checks
+// before anything indexes by label.
+__global__ void k_seg_count(const int32_t* __restrict__ labels, int64_t n, int k, int32_t* __restrict__ chunk_cnt,
+                            int32_t* __restrict__ bad) {
+    extern __shared__ int hist[];
+    for (int j = threadIdx.x; j < k; j += blockDim.x) hist[j] = 0;
+    __syncthreads();
+    const int64_t base = (int64_t)blockIdx.x * SEG_CHUNK;
+    for (int t = threadIdx.x; t < SEG_CHUNK; t += blockDim.x) {
+        int64_t i = base + t;
+        if (i < n) {
+            int l = labels[i];
+            if (l >= 0 && l < k) atomicAdd(&hist[l], 1);
+            else atomicOr(bad, 1);
+        }
+    }
+    __syncthreads();
+    for (int j = threadIdx.x; j < k; j += blockDim.x) chunk_cnt[(size_t)blockIdx.x * k + j] = hist[j];
+}
+
+// one block per cluster: exclusive scan of its per-chunk counts, total -> counts[j]
+__global__ void k_seg_scan_chunks(int32_t* __restrict__ chunk_cnt, int nchunks, int k, int32_t* __restrict__ counts) {
+    __shared__ int red[32];
+    const int j = blockIdx.x;
+    int carry = 0;
+    for (int c0 = 0; c0 < nchunks; c0 += blockDim.x) {
+        int c = c0 + threadIdx.x;
+        int v = c < nchunks ? chunk_cnt[(size_t)c * k + j] : 0;
+        // block inclusive scan
+        int x = v;
+        const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            int y = __shfl_up_sync(0xffffffffu, x, o);
+            if (lane >= o) x += y;
+        }
+        if (lane == 31) red[wid] = x;
+        __syncthreads();
+        if (wid == 0) {
+            int w = lane < (int)(blockDim.x >> 5) ? red[lane] : 0;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                int y = __shfl_up_sync(0xffffffffu, w, o);
+                if (lane >= o) w += y;
+            }
+            red[lane] = w;
+        }
+        __syncthreads();
+        int incl = x + (wid > 0 ? red[wid - 1] : 0);
+        if (c < nchunks) chunk_cnt[(size_t)c * k + j] = carry + incl - v;
+        int total = red[(blockDim.x >> 5) - 1];
+        __syncthreads();
+        carry += total;
+    }
+    if (threadIdx.x == 0) counts[j] = carry;
+}
+
+__global__ void k_seg_offsets(const int32_t* __restrict__ counts, int k, int32_t* __restrict__ offsets,
+                              int32_t* __restrict__ sum_class) {
+    if (threadIdx.x == 0) {
+        int acc = 0, nz = 0;
+        for (int j = 0; j < k; ++j) {
+            offsets[j] = acc;
+            acc += counts[j];
+            nz += counts[j] != 0;
+        }
+        *sum_class = nz;
+    }
+}
+
+__global__ void __launch_bounds__(SEG_BLOCK) k_seg_scatter(const int32_t* __restrict__ labels, int64_t n, int k,
+                                                           const int32_t* __restrict__ chunk_base,
+                                                           const int32_t* __restrict__ offsets,
+                                                           int32_t* __restrict__ perm) {
+    extern __shared__ int sm[];
+    int* running = sm;              // k
+    int* wcnt = sm + k;             // 8 * k
+    const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+    const int64_t base = (int64_t)blockIdx.x * SEG_CHUNK;
+    for (int j = tid; j < k; j += SEG_BLOCK) running[j] = offsets[j] + chunk_base[(size_t)blockIdx.x * k + j];
+    const unsigned lt = (1u << lane) - 1u;
+    for (int r0 = 0; r0 < SEG_CHUNK; r0 += SEG_BLOCK) {
+        for (int e = tid; e < 8 * k; e += SEG_BLOCK) wcnt[e] = 0;
+        __syncthreads();
+        const int64_t i = base + r0 + tid;
+        int lab = i < n ? labels[i] : -1;
+        if (lab >= k) lab = -1;
+        const unsigned peers = __match_any_sync(0xffffffffu, lab);
+        const int rank = __popc(peers & lt);
+        if (lab >= 0 && rank == 0) wcnt[wid * k + lab] = __popc(peers);
+        __syncthreads();
+        if (lab >= 0) {
+            int pos = running[lab] + rank;
+            for (int w = 0; w < wid; ++w) pos += wcnt[w * k + lab];
+            perm[pos] = (int32_t)i;
+        }
+        __syncthreads();
+        for (int j = tid; j < k; j += SEG_BLOCK) {
+            int add = 0;
+#pragma unroll
+            for (int w = 0; w < 8; ++w) add += wcnt[w * k + j];
+            running[j] += add;
+        }
+    }
+}
+
+// ---------------------------------------------------------------- gate
+// compat: thrust::reduce(c, c+m, 0) accumulates in int, truncating each value
+// (shapeExtract.cuh:1131), gate = |sum| > 1e-16; canonical: any non-zero value.
+__global__ void k_gate(const float* __restrict__ C, int m, int mode, uint8_t* __restrict__ gate) {
+    __shared__ double red[32];
+    const float* c = C + (size_t)blockIdx.x * m;
+    double s = 0;
+    for (int t = threadIdx.x; t < m; t += blockDim.x) {
+        float v = c[t];
+        if (mode == TC_MODE_COMPAT) s += (double)(long long)(int)v;  // cvt.rzi saturates
+        else s += (v != 0.f) ? 1.0 : 0.0;
+    }
+    s = block_sum_d(s, red);
+    if (threadIdx.x == 0) gate[blockIdx.x] = (mode == TC_MODE_COMPAT) ? (fabs(s) > 1e-16) : (s > 0);
+}
+
+// ---------------------------------------------------------------- SIMT Gram
+// 64x64 output tiles of the upper triangle, 256 threads x 4x4 outputs, K in
+// 32-row slabs; FP32 sums of 256 rows are folded into a compensated total.
+__global__ void __launch_bounds__(256) k_gram_simt(const float* __restrict__ Y, const int32_t* __restrict__ counts,
+                                                   const int32_t* __restrict__ offsets, int m, int nt,
+                                                   float* __restrict__ S) {
+    __shared__ __align__(16) float As[32][64];
+    __shared__ __align__(16) float Bs[32][64];
+    const int c = blockIdx.y;
+    const int cnt = counts[c];
+    if (cnt == 0) return;
+    int t = blockIdx.x, ta = 0;
+    while (t >= nt - ta) { t -= nt - ta; ++ta; }
+    const int tb = ta + t;
+    const int a0 = ta * 64, b0 = tb * 64;
+    const float* Yc = Y + (size_t)offsets[c] * m;
+    const int tid = threadIdx.x, tx = tid & 15, ty = tid >> 4;
+    float acc[4][4], tot[4][4], cmp[4][4];
+#pragma unroll
+    for (int i = 0; i < 4; ++i)
+#pragma unroll
+        for (int j = 0; j < 4; ++j) acc[i][j] = tot[i][j] = cmp[i][j] = 0.f;
+    int slab = 0;
+    for (int k0 = 0; k0 < cnt; k0 += 32, ++slab) {
+#pragma unroll
+        for (int e = 0; e < 8; ++e) {
+            int idx = tid + e * 256;
+            int kk = idx >> 6, ii = idx & 63;
+            int row = k0 + kk;
+            bool ok = row < cnt;
+            As[kk][ii] = (ok && a0 + ii < m) ? Yc[(size_t)row * m + a0 + ii] : 0.f;
+            Bs[kk][ii] = (ok && b0 + ii < m) ? Yc[(size_t)row * m + b0 + ii] : 0.f;
+        }
+        __syncthreads();
+#pragma unroll 8
+        for (int kk = 0; kk < 32; ++kk) {
+            float4 av = *reinterpret_cast<const float4*>(&As[kk][ty * 4]);
+            float4 bv = *reinterpret_cast<const float4*>(&Bs[kk][tx * 4]);
+            float a[4] = {av.x, av.y, av.z, av.w}, b[4] = {bv.x, bv.y, bv.z, bv.w};
+#pragma unroll
+            for (int i = 0; i < 4; ++i)
+#pragma unroll
+                for (int j = 0; j < 4; ++j) acc[i][j] = fmaf(a[i], b[j], acc[i][j]);
+        }
+        __syncthreads();
+        if ((slab & 7) == 7 || k0 + 32 >= cnt) {
+#pragma unroll
+            for (int i = 0; i < 4; ++i)
+#pragma unroll
+                for (int j = 0; j < 4; ++j) {  // Kahan: tot += acc
+                    float y = acc[i][j] - cmp[i][j];
+                    float tt = tot[i][j] + y;
+                    cmp[i][j] = (tt - tot[i][j]) - y;
+                    tot[i][j] = tt;
+                    acc[i][j] = 0.f;
+                }
+        }
+    }
+    float* Sc = S + (size_t)c * m * m;
+#pragma unroll
+    for (int i = 0; i < 4; ++i)
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            int a = a0 + ty * 4 + i, b = b0 + tx * 4 + j;
+            if (a < m && b < m) {
+                Sc[(size_t)a * m + b] = tot[i][j];
+                Sc[(size_t)b * m + a] = tot[i][j];
+            }
+        }
+}
+
+// ---------------------------------------------------------------- centring terms
+// r[c][a] = sum_b S[c][a][b] (FP64), tot[c] = sum_a r[c][a]
+__global__ void k_rowsum(const float* __restrict__ S, const int32_t* __restrict__ counts, int m,
+                         double* __restrict__ r, double* __restrict__ tot) {
+    const int c = blockIdx.y;
+    if (counts[c] == 0) return;
+    const int lane = threadIdx.x & 31;
+    const int a = blockIdx.x * 8 + (threadIdx.x >> 5);
+    if (a >= m) return;
+    const float* row = S + ((size_t)c * m + a) * m;
+    float s = 0.f;
+    for (int b = lane; b < m; b += 32) s += row[b];
+    double d = s;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) d += __shfl_xor_sync(0xffffffffu, d, o);
+    if (lane == 0) {
+        r[(size_t)c * m + a] = d;
+        atomicAdd(&tot[c], d);
+    }
+}
+
+// ---------------------------------------------------------------- power iteration
+// Step t: v_t = u_t / |u_t|, u_{t+1} = M v_t; u lives in 3 rotating slots.
+// nrm2[slot][c] = |u|^2 (FP64); delta[c] = |v_t - v_{t-1}|.
+__global__ void k_power_prep(const int32_t* __restrict__ counts, int k, int m, float* __restrict__ u,
+                             double* __restrict__ nrm2) {
+    __shared__ double red[32];
+    const int c = blockIdx.x;
+    double s = 0;
+    for (int a = threadIdx.x; a < m; a += blockDim.x) {
+        float v = (a % 2 == 0) ? 1.0f : 0.5f;  // init_vec (shapeExtract.cuh:269-283)
+        u[(size_t)c * m + a] = v;
+        s += (double)v * v;
+    }
+    s = block_sum_d(s, red);
+    if (threadIdx.x == 0) {
+        nrm2[c] = s;          // slot 0
+        nrm2[k + c] = 0.0;    // slot 1: target of step 0
+        nrm2[2 * k + c] = 0.0;
+    }
+}
+
+constexpr int PW_ROWS = 32;  // rows per block (8 warps x 4)
+
+__global__ void __launch_bounds__(256) k_power_step(const float* __restrict__ S, const double* __restrict__ r,
+                                                    const double* __restrict__ tot, const int32_t* __restrict__ counts,
+                                                    int k, int m, int t, float* __restrict__ u,
+                                                    double* __restrict__ nrm2, double* __restrict__ delta) {
+    extern __shared__ float vs[];  // m
+    __shared__ double red[32];
+    const int c = blockIdx.y;
+    if (counts[c] == 0) return;
+    const int cur = t % 3, nxt = (t + 1) % 3, prv = (t + 2) % 3;
+    const float* ucur = u + ((size_t)cur * k + c) * m;
+    const double ncur = nrm2[(size_t)cur * k + c];
+    const float inv = ncur > 0 ? (float)(1.0 / sqrt(ncur)) : __int_as_float(0x7fc00000);
+    double sv = 0, rv = 0;
+    const double* rc = r + (size_t)c * m;
+    for (int a = threadIdx.x; a < m; a += blockDim.x) {
+        float v = ucur[a] * inv;
+        vs[a] = v;
+        sv += v;
+        rv += rc[a] * (double)v;
+    }
+    sv = block_sum_d(sv, red);
+    rv = block_sum_d(rv, red);
+    if (blockIdx.x == 0) {
+        double dd = 0;
+        if (t >= 1) {
+            const float* uprv = u + ((size_t)prv * k + c) * m;
+            const double np = nrm2[(size_t)prv * k + c];
+            const float ip = np > 0 ? (float)(1.0 / sqrt(np)) : 0.f;
+            for (int a = threadIdx.x; a < m; a += blockDim.x) {
+                double d = (double)vs[a] - (double)(uprv[a] * ip);
+                dd += d * d;
+            }
+        }
+        dd = block_sum_d(dd, red);
+        if (threadIdx.x == 0) {
+            delta[c] = t >= 1 ? sqrt(dd) : 1.0;
+            nrm2[(size_t)prv * k + c] = 0.0;  // target of step t+1
+        }
+    }
+    __syncthreads();
+    const double mm = (double)m;
+    const double corr_const = -rv / mm + tot[c] * sv / (mm * mm);
+    const double corr_r = -sv / mm;
+    const float* Sc = S + (size_t)c * m * m;
+    float* unxt = u + ((size_t)nxt * k + c) * m;
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    double local = 0;
+    for (int q = 0; q < PW_ROWS / 8; ++q) {
+        const int a = blockIdx.x * PW_ROWS + wid * (PW_ROWS / 8) + q;
+        if (a >= m) break;
+        const float* row = Sc + (size_t)a * m;
+        float s = 0.f;
+        for (int b = lane; b < m; b += 32) s = fmaf(row[b], vs[b], s);
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+        if (lane == 0) {
+            double y = (double)s + corr_r * rc[a] + corr_const;
+            float yf = (float)y;
+            unxt[a] = yf;
+            local += (double)yf * yf;
+        }
+    }
+    local = block_sum_d(local, red);
+    if (threadIdx.x == 0) atomicAdd(&nrm2[(size_t)nxt * k + c], local);
+}
+
+// v = u_T/|u_T|, lambda = v . u_{T+1} (FP64).  lambda > 0: sign rule against the
+// cluster's first member a (flip when |a - v| >= |a + v|) and store (canonical:
+// re-z-normalised, ddof=1).  lambda <= 0 (M numerically zero): the last basis
+// vector - the last column of a symmetric eigensolver's identity basis - with the
+// same sign rule.  NaN: the centroid is left unchanged (neither branch of
+// shapeExtract.cuh:638-649 fires).
+__global__ void k_power_final(const float* __restrict__ u, const double* __restrict__ nrm2,
+                              const int32_t* __restrict__ counts, const int32_t* __restrict__ offsets,
+                              const float* __restrict__ seg, int k, int m, int T, int mode,
+                              float* __restrict__ C, float* __restrict__ lambda_out) {
+    __shared__ double red[32];
+    __shared__ double sh_lam, sh_flip, sh_mean, sh_inv;
+    const int c = blockIdx.x;
+    if (counts[c] == 0) return;
+    const int sT = T % 3, sN = (T + 1) % 3;
+    const float* uT = u + ((size_t)sT * k + c) * m;
+    const float* uN = u + ((size_t)sN * k + c) * m;
+    const double nT = nrm2[(size_t)sT * k + c];
+    const double invT = 1.0 / sqrt(nT);
+    const float* a = seg + (size_t)offsets[c] * m;
+    double lam = 0;
+    for (int i = threadIdx.x; i < m; i += blockDim.x) lam += (double)((float)(uT[i] * invT)) * (double)uN[i];
+    lam = block_sum_d(lam, red);
+    if (threadIdx.x == 0) sh_lam = lam;
+    __syncthreads();
+    lam = sh_lam;
+    if (!(lam > 0) && !(lam <= 0)) return;  // NaN
+    const bool degenerate = !(lam > 0);
+    double d1 = 0, d2 = 0, sum = 0;
+    for (int i = threadIdx.x; i < m; i += blockDim.x) {
+        double v = degenerate ? (i == m - 1 ? 1.0 : 0.0) : (double)((float)(uT[i] * invT));
+        double ai = a[i];
+        d1 += (ai - v) * (ai - v);
+        d2 += (ai + v) * (ai + v);
+        sum += v;
+    }
+    d1 = block_sum_d(d1, red);
+    d2 = block_sum_d(d2, red);
+    sum = block_sum_d(sum, red);
+    const double sgn = (sqrt(d1) >= sqrt(d2)) ? -1.0 : 1.0;
+    double mean = 0, inv = 1;
+    if (mode == TC_MODE_CANONICAL) {
+        mean = sgn * sum / m;
+        double ss = 0;
+        for (int i = threadIdx.x; i < m; i += blockDim.x) {
+            double v = sgn * (degenerate ? (i == m - 1 ? 1.0 : 0.0) : (double)((float)(uT[i] * invT)));
+            ss += (v - mean) * (v - mean);
+        }
+        ss = block_sum_d(ss, red);
+        double sd = sqrt(ss / (m - 1));
+        inv = sd > 0 ? 1.0 / sd : 0.0;
+    }
+    float* out = C + (size_t)c * m;
+    for (int i = threadIdx.x; i < m; i += blockDim.x) {
+        double v = sgn * (degenerate ? (i == m - 1 ? 1.0 : 0.0) : (double)((float)(uT[i] * invT)));
+        out[i] = (float)((v - mean) * inv);
+    }
+    if (threadIdx.x == 0 && lambda_out) lambda_out[c] = (float)lam;
+}
+
+// ---------------------------------------------------------------- driver
+int run_extract(tc_ctx* ctx, const ExtractArgs& a, cudaStream_t s) {
+    Workspace& ws = ctx->ws;
+    const int64_t n = a.n;
+    const int m = a.m, k = a.k;
+    TC_REQUIRE(k >= 1 && k <= MAX_K, TC_ERR_UNSUPPORTED, "k must be in [1, 1024]");
+    TC_REQUIRE(m >= 2 && m <= 8192, TC_ERR_UNSUPPORTED, "series length must be in [2, 8192]");
+    const int nchunks = ceil_div(n, SEG_CHUNK);
+    int32_t* perm = ws.perm.as<int32_t>(std::max<int64_t>(n, 1));
+    int32_t* chunk = ws.chunk_counts.as<int32_t>((size_t)std::max(nchunks, 1) * k);
+    int32_t* counts = a.counts ? a.counts : ws.counts.as<int32_t>(k);
+    int32_t* offsets = ws.offsets.as<int32_t>(k);
+    uint8_t* gate = ws.gate.as<uint8_t>(k);
+    int32_t* scal = ws.scal.as<int32_t>(16);
+    float* seg = ws.seg.as<float>((size_t)std::max<int64_t>(n, 1) * m);
+    float* S = ws.gram.as<float>((size_t)k * m * m);
+    double* rs = ws.rowsum.as<double>((size_t)k * m + k);
+    double* tot = rs + (size_t)k * m;
+    float* u = ws.piter.as<float>((size_t)3 * k * m);
+    double* st = ws.pstats.as<double>((size_t)4 * k);
+    double* nrm2 = st;
+    double* delta = st + 3 * k;
+
+    TC_CUDA(cudaMemsetAsync(scal, 0, sizeof(int32_t) * 16, s));
+    if (n > 0) {
+        k_seg_count<<<nchunks, SEG_BLOCK, k * sizeof(int), s>>>(a.labels, n, k, chunk, scal + 1);
+        TC_CHECK_LAUNCH();
+    } else {
+        TC_CUDA(cudaMemsetAsync(chunk, 0, sizeof(int32_t) * k, s));
+    }
+    k_seg_scan_chunks<<<k, 256, 0, s>>>(chunk, std::max(nchunks, 1), k, counts);
+    TC_CHECK_LAUNCH();
+    k_seg_offsets<<<1, 32, 0, s>>>(counts, k, offsets, scal);
+    TC_CHECK_LAUNCH();
+    if (n > 0) {
+        size_t smem = (size_t)9 * k * sizeof(int);
+        TC_CUDA(cudaFuncSetAttribute(k_seg_scatter, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        k_seg_scatter<<<nchunks, SEG_BLOCK, smem, s>>>(a.labels, n, k, chunk, offsets, perm);
+        TC_CHECK_LAUNCH();
+    }
+    k_gate<<<k, 256, 0, s>>>(a.C, m, a.mode, gate);
+    TC_CHECK_LAUNCH();
+
+    // one small read-back: counts, gates, sum_class
+    std::vector<int32_t> h_counts(k);
+    std::vector<uint8_t> h_gate(k);
+    int32_t h_sc[2] = {0, 0};
+    TC_CUDA(cudaMemcpyAsync(h_counts.data(), counts, sizeof(int32_t) * k, cudaMemcpyDeviceToHost, s));
+    TC_CUDA(cudaMemcpyAsync(h_gate.data(), gate, k, cudaMemcpyDeviceToHost, s));
+    TC_CUDA(cudaMemcpyAsync(h_sc, scal, sizeof(int32_t) * 2, cudaMemcpyDeviceToHost, s));
+    TC_CUDA(cudaStreamSynchronize(s));
+    TC_REQUIRE(h_sc[1] == 0, TC_ERR_ARG, "a label is outside [0, k)");
+    bool any_gate = false;
+    for (int j = 0; j < k; ++j) any_gate |= (h_gate[j] && h_counts[j] > 0);
+
+    const int32_t* shift = a.shift;
+    if (any_gate && !shift) {
+        // alignment shifts of each series against its own centroid (sbd3D, SBD.cuh:69-85)
+        const int F = fft_size(m, a.mode);
+        float2* spec = ws.spectra.as<float2>((size_t)k * (F / 2 + 1));
+        launch_centroid_spectra(ctx, a.C, k, m, F, spec, s);
+        int32_t* sh = ws.shift.as<int32_t>(std::max<int64_t>(n, 1));
+        AssignArgs aa{};
+        aa.x = a.x;
+        aa.spec = spec;
+        aa.n = n;
+        aa.m = m;
+        aa.k = k;
+        aa.F = F;
+        aa.clamp2 = 0;
+        aa.fixed = a.labels;
+        aa.shift = sh;
+        launch_assign_fft(ctx, aa, s);
+        shift = sh;
+    }
+    launch_gather_norm(a.x, perm, a.labels, any_gate ? shift : nullptr, any_gate ? gate : nullptr, n, m, seg,
+                       ctx->sm_count, s);
+
+    // Gram
+    const int nt = ceil_div(m, 64);
+    if (gram_tc_supported(m, a.precision)) {
+        launch_gram_tc(ctx, seg, counts, offsets, k, m, a.precision, S, s);
+    } else {
+        dim3 g(nt * (nt + 1) / 2, k);
+        k_gram_simt<<<g, 256, 0, s>>>(seg, counts, offsets, m, nt, S);
+        TC_CHECK_LAUNCH();
+    }
+    TC_CUDA(cudaMemsetAsync(tot, 0, sizeof(double) * k, s));
+    k_rowsum<<<dim3(ceil_div(m, 8), k), 256, 0, s>>>(S, counts, m, rs, tot);
+    TC_CHECK_LAUNCH();
+
+    // power iteration: compat runs at most m steps (the reference's fixed count),
+    // stopping early once every cluster's step difference is at FP32 noise level;
+    // cal_select=1 / canonical converge fully (the reference's syevd result).
+    const bool full = a.cal_select || a.mode == TC_MODE_CANONICAL;
+    const int tmax = full ? std::max(4 * m, 200) : m;
+    const double tol = full ? 5e-7 : 1e-6;
+    k_power_prep<<<k, 256, 0, s>>>(counts, k, m, u, nrm2);
+    TC_CHECK_LAUNCH();
+    const dim3 pg(ceil_div(m, PW_ROWS), k);
+    const size_t psm = sizeof(float) * m;
+    if (psm > 48 * 1024)
+        TC_CUDA(cudaFuncSetAttribute(k_power_step, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)psm));
+    std::vector<double> h_delta(k);
+    int T = tmax;
+    for (int t = 0; t <= tmax; ++t) {
+        k_power_step<<<pg, 256, psm, s>>>(S, rs, tot, counts, k, m, t, u, nrm2, delta);
+        TC_CHECK_LAUNCH();
+        if (t == tmax) break;
+        if (t >= 1 && (t % 8 == 0)) {
+            TC_CUDA(cudaMemcpyAsync(h_delta.data(), delta, sizeof(double) * k, cudaMemcpyDeviceToHost, s));
+            TC_CUDA(cudaStreamSynchronize(s));
+            double mx = 0;
+            for (int j = 0; j < k; ++j)
+                if (h_counts[j] > 0) mx = std::max(mx, h_delta[j]);
+            if (mx < tol) {
+                T = t;
+                break;
+            }
+        }
+    }
+    k_power_final<<<k, 256, 0, s>>>(u, nrm2, counts, offsets, seg, k, m, T, a.mode, a.C, nullptr);
+    TC_CHECK_LAUNCH();
+    return h_sc[0];
+}
+
+}  // namespace tc

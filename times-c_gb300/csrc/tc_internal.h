@@ -1,0 +1,142 @@
+// Internal declarations shared by the engine's translation units.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <cstdio>
+#include <string>
+#include <vector>
+
+#include "timesc.h"
+
+// ---------------------------------------------------------------- errors
+struct TcError {
+    int code;
+    std::string msg;
+};
+
+#define TC_CUDA(call)                                                                   \
+    do {                                                                                \
+        cudaError_t e_ = (call);                                                        \
+        if (e_ != cudaSuccess)                                                          \
+            throw TcError{TC_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_)}; \
+    } while (0)
+
+#define TC_CHECK_LAUNCH() TC_CUDA(cudaGetLastError())
+
+#define TC_REQUIRE(cond, code, text)                         \
+    do {                                                     \
+        if (!(cond)) throw TcError{(code), std::string(text)}; \
+    } while (0)
+
+// ---------------------------------------------------------------- device buffers
+// A grow-only device allocation owned by a context.
+struct DevBuf {
+    void* p = nullptr;
+    size_t bytes = 0;
+    void* get(size_t need) {
+        if (need <= bytes) return p;
+        if (p) cudaFree(p);
+        p = nullptr;
+        bytes = 0;
+        if (need == 0) return nullptr;
+        cudaError_t e = cudaMalloc(&p, need);
+        if (e != cudaSuccess) {
+            cudaGetLastError();
+            throw TcError{TC_ERR_NOMEM, "cudaMalloc of " + std::to_string(need) + " bytes failed"};
+        }
+        bytes = need;
+        return p;
+    }
+    template <class T>
+    T* as(size_t count) { return static_cast<T*>(get(count * sizeof(T))); }
+    void release() {
+        if (p) cudaFree(p);
+        p = nullptr;
+        bytes = 0;
+    }
+};
+
+// Twiddle tables for one FFT length F (N = F/2 complex points):
+//   twN[e] = exp(-2 pi i e / N), twF[f] = exp(-2 pi i f / F), e, f in [0, N)
+struct FftTables {
+    int F = 0;
+    DevBuf twN, twF;
+};
+
+// Per-iteration working set of the k-Shape loop and the stage entry points.
+struct Workspace {
+    DevBuf x;            // normalised series, n*m f32 (whole-loop runs)
+    DevBuf labels, old_labels, shift, dist;
+    DevBuf centroids, spectra;  // k*m f32; k*(N+1) float2
+    DevBuf seg;          // aligned, re-normalised members in cluster order, n*m (f32 or bf16)
+    DevBuf perm, chunk_counts, counts, offsets, gate, scal;
+    DevBuf gram;         // k*m*m f32
+    DevBuf rowsum;       // k*m f64 + k f64
+    DevBuf piter;        // power-iteration vectors 3*k*m f32
+    DevBuf pstats;       // 3*k*4 f64
+    DevBuf aux;          // small scalars (changed count, dist sum, sum_class, flags)
+    DevBuf toeplitz;     // bf16 shifted centroid copies for the tensor-core correlation
+    DevBuf xbf;          // bf16 copy of the series for the tensor-core correlation
+};
+
+struct tc_ctx {
+    int device = 0;
+    int sm_count = 0;
+    size_t smem_optin = 0;
+    std::string last_error;
+    std::vector<FftTables*> fft;  // cached per F
+    Workspace ws;
+    cudaStream_t own_stream = nullptr;
+};
+
+namespace tc {
+
+// ---------------------------------------------------------------- launch helpers (defined in .cu files)
+const FftTables& fft_tables(tc_ctx* ctx, int F);
+
+void launch_znorm(float* x, int64_t n, int m, int ddof, int sm_count, cudaStream_t s);
+void launch_init_labels(int32_t* labels, int64_t n, int k, cudaStream_t s);
+
+// centroid spectra: spec[j][f] = conj-free spectrum of c_j scaled by 1/(2N |c_j|), f in [0, N]
+void launch_centroid_spectra(tc_ctx* ctx, const float* C, int k, int m, int F, float2* spec, cudaStream_t s);
+
+struct AssignArgs {
+    const float* x;
+    const float2* spec;        // k*(N+1)
+    int64_t n;
+    int m, k, F;
+    int clamp2;                // pad value 2 of get_pos_idx (compat, 2m-1 < 512)
+    const int32_t* fixed;      // if set: evaluate only centroid fixed[i] (alignment shifts)
+    int32_t* labels;
+    float* dist;
+    int32_t* shift;
+    const int32_t* old_labels;
+    int32_t* changed;
+    double* dist_sum;
+};
+void launch_assign_fft(tc_ctx* ctx, const AssignArgs& a, cudaStream_t s);
+
+// tensor-core correlation (tcgen05); returns false when the shape is not supported
+bool tc_assign_supported(int m, int F, int k, int precision);
+void launch_assign_tc(tc_ctx* ctx, const AssignArgs& a, int precision, cudaStream_t s);
+
+// extraction
+struct ExtractArgs {
+    const float* x;
+    const int32_t* labels;
+    const int32_t* shift;      // may be null when no gate is set
+    float* C;
+    int64_t n;
+    int m, k, mode, cal_select, precision;
+    int32_t* counts;           // k
+};
+// returns sum_class (synchronises)
+int run_extract(tc_ctx* ctx, const ExtractArgs& a, cudaStream_t s);
+
+// helpers
+inline int ceil_div(int64_t a, int64_t b) { return (int)((a + b - 1) / b); }
+int fft_size(int m, int mode);
+
+}  // namespace tc

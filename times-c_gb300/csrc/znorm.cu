@@ -1,0 +1,166 @@
+// Row z-normalisation: x <- (x - mean) / sqrt(sum (x-mean)^2 / (m - ddof)).
+//
+// Replaces z_norm_gpu_x (normalization.cuh:150-177: a cuBLAS row-mean GEMM, a
+// rank-1 subtract, then a 1024-thread block per row).  Here one warp owns one
+// row held in registers (one block per row for m > 1024): a single HBM read and
+// write per value, FP32 lane partials combined in FP64 across the warp/block.
+// The GATHER variant is the extraction's fused pass: it reads row perm[pos]
+// shifted by its alignment shift (out[t] = x[t - shift], zero fill, SBD.cuh:14-29)
+// and writes the normalised row to position pos of the cluster-ordered buffer
+// (block_alloc2D + sbd3D + z_norm_gpu_x of shapeExtract.cuh:1117-1141).
+#include "tc_internal.h"
+
+namespace tc {
+
+__device__ __forceinline__ double warp_sum_d(double v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+struct RowSrc {
+    const float* x;
+    int shift;
+};
+
+template <bool GATHER>
+__device__ __forceinline__ RowSrc row_source(const float* src, int64_t row, int m, const int32_t* perm,
+                                             const int32_t* labels, const int32_t* shift, const uint8_t* gate) {
+    RowSrc r;
+    if (GATHER) {
+        int64_t i = perm[row];
+        r.x = src + (size_t)i * m;
+        r.shift = (gate && shift && gate[labels[i]]) ? shift[i] : 0;
+    } else {
+        r.x = src + (size_t)row * m;
+        r.shift = 0;
+    }
+    return r;
+}
+
+template <int VPL, bool GATHER>
+__global__ void __launch_bounds__(256) k_norm_rows_warp(const float* __restrict__ src, float* dst, int64_t n, int m,
+                                                        int ddof, const int32_t* __restrict__ perm,
+                                                        const int32_t* __restrict__ labels,
+                                                        const int32_t* __restrict__ shift,
+                                                        const uint8_t* __restrict__ gate) {
+    const int lane = threadIdx.x & 31;
+    const int64_t w0 = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    for (int64_t row = w0; row < n; row += nw) {
+        RowSrc rs = row_source<GATHER>(src, row, m, perm, labels, shift, gate);
+        float v[VPL];
+        float s = 0.f;
+#pragma unroll
+        for (int q = 0; q < VPL; ++q) {
+            int t = lane + 32 * q;
+            int a = t - rs.shift;
+            v[q] = (t < m && a >= 0 && a < m) ? rs.x[a] : 0.f;
+            s += v[q];
+        }
+        const float mean = (float)(warp_sum_d((double)s) / m);
+        float ss = 0.f;
+#pragma unroll
+        for (int q = 0; q < VPL; ++q) {
+            int t = lane + 32 * q;
+            float d = t < m ? v[q] - mean : 0.f;
+            v[q] = d;
+            ss += d * d;
+        }
+        const double sd = sqrt(warp_sum_d((double)ss) / (double)(m - ddof));
+        const float inv = (sd > 0.0 && isfinite(sd)) ? (float)(1.0 / sd) : 0.f;
+        float* y = dst + (size_t)row * m;
+#pragma unroll
+        for (int q = 0; q < VPL; ++q) {
+            int t = lane + 32 * q;
+            if (t < m) y[t] = v[q] * inv;
+        }
+    }
+}
+
+template <int VPT, bool GATHER>
+__global__ void __launch_bounds__(256) k_norm_rows_block(const float* __restrict__ src, float* dst, int64_t n, int m,
+                                                         int ddof, const int32_t* __restrict__ perm,
+                                                         const int32_t* __restrict__ labels,
+                                                         const int32_t* __restrict__ shift,
+                                                         const uint8_t* __restrict__ gate) {
+    __shared__ double red[8];
+    const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+    for (int64_t row = blockIdx.x; row < n; row += gridDim.x) {
+        RowSrc rs = row_source<GATHER>(src, row, m, perm, labels, shift, gate);
+        float v[VPT];
+        float s = 0.f;
+#pragma unroll
+        for (int q = 0; q < VPT; ++q) {
+            int t = tid + 256 * q;
+            int a = t - rs.shift;
+            v[q] = (t < m && a >= 0 && a < m) ? rs.x[a] : 0.f;
+            s += v[q];
+        }
+        double ds = warp_sum_d((double)s);
+        if (lane == 0) red[wid] = ds;
+        __syncthreads();
+        ds = 0;
+#pragma unroll
+        for (int w = 0; w < 8; ++w) ds += red[w];
+        __syncthreads();
+        const float mean = (float)(ds / m);
+        float ss = 0.f;
+#pragma unroll
+        for (int q = 0; q < VPT; ++q) {
+            int t = tid + 256 * q;
+            float d = t < m ? v[q] - mean : 0.f;
+            v[q] = d;
+            ss += d * d;
+        }
+        double dss = warp_sum_d((double)ss);
+        if (lane == 0) red[wid] = dss;
+        __syncthreads();
+        dss = 0;
+#pragma unroll
+        for (int w = 0; w < 8; ++w) dss += red[w];
+        __syncthreads();
+        const double sd = sqrt(dss / (double)(m - ddof));
+        const float inv = (sd > 0.0 && isfinite(sd)) ? (float)(1.0 / sd) : 0.f;
+        float* y = dst + (size_t)row * m;
+#pragma unroll
+        for (int q = 0; q < VPT; ++q) {
+            int t = tid + 256 * q;
+            if (t < m) y[t] = v[q] * inv;
+        }
+    }
+}
+
+template <bool GATHER>
+static void norm_rows(const float* src, float* dst, int64_t n, int m, int ddof, const int32_t* perm,
+                      const int32_t* labels, const int32_t* shift, const uint8_t* gate, int sm_count,
+                      cudaStream_t s) {
+    if (n == 0) return;
+    TC_REQUIRE(m >= 2 && m <= 8192, TC_ERR_UNSUPPORTED, "series length must be in [2, 8192]");
+    const int wgrid = (int)std::min<int64_t>(ceil_div(n, 8), (int64_t)sm_count * 16);
+    const int bgrid = (int)std::min<int64_t>(n, (int64_t)sm_count * 8);
+#define WARP(VPL) k_norm_rows_warp<VPL, GATHER><<<wgrid, 256, 0, s>>>(src, dst, n, m, ddof, perm, labels, shift, gate)
+#define BLOCK(VPT) k_norm_rows_block<VPT, GATHER><<<bgrid, 256, 0, s>>>(src, dst, n, m, ddof, perm, labels, shift, gate)
+    if (m <= 64) WARP(2);
+    else if (m <= 128) WARP(4);
+    else if (m <= 256) WARP(8);
+    else if (m <= 512) WARP(16);
+    else if (m <= 1024) WARP(32);
+    else if (m <= 2048) BLOCK(8);
+    else if (m <= 4096) BLOCK(16);
+    else BLOCK(32);
+#undef WARP
+#undef BLOCK
+    TC_CHECK_LAUNCH();
+}
+
+void launch_znorm(float* x, int64_t n, int m, int ddof, int sm_count, cudaStream_t s) {
+    norm_rows<false>(x, x, n, m, ddof, nullptr, nullptr, nullptr, nullptr, sm_count, s);
+}
+
+void launch_gather_norm(const float* x, const int32_t* perm, const int32_t* labels, const int32_t* shift,
+                        const uint8_t* gate, int64_t n, int m, float* seg, int sm_count, cudaStream_t s) {
+    norm_rows<true>(x, seg, n, m, 1, perm, labels, shift, gate, sm_count, s);
+}
+
+}  // namespace tc
