@@ -1,0 +1,344 @@
+"""k-Shape benchmark on GB300.
+
+Workload (default): the precision configuration of the Times-C baseline,
+n = 1,000,000 series, m = 512, k = 32, synthetic data (the prototype generator
+of times-c_gb300/csrc/gen.cpp, noise 0.3).  A step is one whole k-Shape
+iteration in the reference's loop order (extract shapes -> SBD assignment ->
+convergence read-back) over all series, with the series resident in HBM.
+
+  value      SBD pairs/s = n*k / (iteration time), whole iterations
+  e2e        the same through tc_kshape_run with pinned host buffers
+             (host->device copy of the series, z-norm, loop, labels and
+             centroids back), pairs/s = n*k*iterations / wall time
+  roofline   the dominant kernel (the fused SBD assignment), CUDA events on
+             the launching stream; algorithmic work per launch as documented
+             in the design doc
+  cpu_baseline  the FP64 oracle (a restatement, "port") on the host cores,
+             one iteration on a bounded sample of the same workload
+
+`--impl reference` times the reference's CPU implementation of the path.  Its
+own CPU code (Code/test/test_timesC.py) is not present on GPU hosts, so the
+FP64 port of it (oracle/) runs instead, on all host threads.
+
+Multi-GPU: the path is run as independent replicas (one per rank).
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+PKG = os.path.join(ROOT, "times-c_gb300")
+for p in (ROOT, PKG):
+    if p not in sys.path:
+        sys.path.insert(0, p)
+
+import numpy as np  # noqa: E402
+
+WORKLOADS = {
+    # name: (n, m, k, noise, dirichlet, description)
+    "c3": (1_000_000, 512, 32, 0.3, 0.0, "precision form: n=1e6 m=512 k=32, FP32 series, noise 0.3"),
+    "c2": (20_000, 2709, 8, 0.2, 2.0, "at scale: n=2e4 m=2709 k=8, Dirichlet(2) classes"),
+    "c1": (300, 128, 4, 0.2, 0.0, "CPU-runnable: n=300 m=128 k=4"),
+}
+PREC = {"fp32": 0, "bf16": 1, "tf32": 2}
+MODES = {"compat": 0, "canonical": 1}
+
+
+def fft_flops(n, k, F):
+    """Algorithmic FP32 flops of the FFT-form assignment (per launch)."""
+    L = int(np.log2(F))
+    return n * (2.5 * F * L) + n * k * (6 * (F // 2 + 1) + 2.5 * F * L + F)
+
+
+def assign_bytes(n, m, k):
+    """Irreducible HBM bytes of one assignment: series in, centroids in, label/dist/shift out."""
+    return 4 * n * m + 4 * k * m + 12 * n
+
+
+def load_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        d = json.load(open(p))
+        return d.get("hbm_gbs", 6800.0), d.get("bf16_tflops", 1900.0), "measured"
+    return 6800.0, 1900.0, "fallback"
+
+
+def profiled_traffic(workload, mode, prec):
+    """dram bytes per launch of the assignment kernel from the committed ncu summary."""
+    p = os.path.join(ROOT, "profiles", "assign_%s_%s_%s.txt" % (prec, workload, mode))
+    if not os.path.exists(p):
+        return None
+    for line in open(p):
+        if line.startswith("traffic_bytes_per_launch:"):
+            try:
+                return float(line.split(":", 1)[1])
+            except ValueError:
+                return None
+    return None
+
+
+class Clocks:
+    """nvidia-smi sampling during the timed region."""
+    Q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+        try:
+            self.p = subprocess.Popen(["nvidia-smi", "-i", str(device), "--query-gpu=" + self.Q,
+                                       "--format=csv,noheader,nounits", "-lms", "200"],
+                                      stdout=self.f, stderr=subprocess.DEVNULL)
+        except OSError:
+            self.p = None
+
+    def stop(self):
+        if self.p is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.p.terminate()
+        self.p.wait()
+        self.f.flush()
+        rows = []
+        for line in open(self.f.name):
+            parts = [t.strip() for t in line.split(",")]
+            if len(parts) == 7:
+                rows.append(parts)
+        os.unlink(self.f.name)
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        sm = [float(r[0]) for r in rows if r[0].replace(".", "").isdigit()]
+        mx = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[j] for r in rows for j in range(4) if r[3 + j].lower() == "active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(rows)}
+
+
+def cpu_iteration(O, X, C, labels, mode, F, ns):
+    m = X.shape[1]
+    om = O.MODE_COMPAT if mode == 0 else O.MODE_CANONICAL
+    t0 = time.perf_counter()
+    Cs, _, _ = O.extract(X[:ns], labels[:ns], C, om)
+    O.assign(X[:ns], Cs, F, clamp2=(mode == 0 and 2 * m - 1 < 512))
+    return time.perf_counter() - t0
+
+
+def cpu_sample_iteration(O, X, C, labels, mode, F, target_s, n_full):
+    """Oracle iterations (extract + assign) on two sample sizes; the iteration
+    time at n_full series is extrapolated linearly (the eigenvector step costs
+    the same at any n, the rest grows with n)."""
+    n = X.shape[0]
+    ns = min(n, 1024)
+    while True:
+        dt = cpu_iteration(O, X, C, labels, mode, F, ns)
+        if dt >= 0.5 * target_s or ns >= n:
+            break
+        ns = min(n, int(ns * max(2.0, 0.7 * target_s / max(dt, 1e-3))))
+    dt_half = cpu_iteration(O, X, C, labels, mode, F, ns // 2)
+    slope = max(dt - dt_half, 1e-9) / (ns - ns // 2)
+    fixed = max(dt - slope * ns, 0.0)
+    return ns, dt, fixed + slope * n_full
+
+
+def host_threads():
+    try:
+        return len(os.sched_getaffinity(0))
+    except AttributeError:
+        return os.cpu_count() or 1
+
+
+def run_reference(args, wl):
+    """The reference's CPU implementation of the path (FP64 port), rank 0 only."""
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    import timesc
+    from oracle import oracle as O
+    n, m, k, noise, dirich, desc = wl
+    os.environ.setdefault("OMP_NUM_THREADS", str(host_threads()))
+    data, truth = timesc.generate(n, m, k, noise=noise, dirichlet=dirich, seed=0)
+    X = O.znorm(data[: min(n, 200_000)].astype(np.float64))
+    rng = np.random.default_rng(0)
+    labels = rng.integers(0, k, size=X.shape[0]).astype(np.int32)
+    C = X[rng.choice(X.shape[0], k, replace=False)].copy()
+    C /= np.linalg.norm(C, axis=1, keepdims=True)
+    md = MODES[args.mode]
+    F = O.fft_size(m, md)
+    ns, _, _ = cpu_sample_iteration(O, X, C, labels, md, F, target_s=3.0, n_full=n)
+    half = cpu_iteration(O, X, C, labels, md, F, ns // 2)
+    full_est = []
+    for s in range(args.warmup + args.steps):
+        dt = cpu_iteration(O, X, C, labels, md, F, ns)
+        slope = max(dt - half, 1e-9) / (ns - ns // 2)
+        if s >= args.warmup:
+            full_est.append(max(dt - slope * ns, 0.0) + slope * n)
+    t = statistics.mean(full_est)
+    value = n * k / t
+    line = {"impl": "reference", "metric": "SBD pairs/s (whole k-Shape iterations)", "value": value,
+            "unit": "pairs/s", "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": 1e3 * t, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": desc, "mode": args.mode, "sample_series": ns},
+            "cpu_baseline": {"value": value, "unit": "pairs/s", "cores": int(os.environ["OMP_NUM_THREADS"]),
+                             "kind": "port",
+                             "sample": "per step one extract+assign of the FP64 oracle on %d of %d series (all %d "
+                                       "centroids); full-n time extrapolated from %d and %d series"
+                                       % (ns, n, k, ns, ns // 2)},
+            "e2e": {"value": value, "unit": "pairs/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="c3", choices=sorted(WORKLOADS))
+    ap.add_argument("--precision", default="fp32", choices=sorted(PREC))
+    ap.add_argument("--mode", default="compat", choices=sorted(MODES))
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
+    wl = WORKLOADS[args.workload]
+    if args.impl == "reference":
+        return run_reference(args, wl)
+
+    import torch
+    import timesc
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+
+    n, m, k, noise, dirich, desc = wl
+    mode, prec = MODES[args.mode], PREC[args.precision]
+    F = timesc.fft_size(m, mode)
+    data, truth = timesc.generate(n, m, k, noise=noise, dirichlet=dirich, seed=rank)
+    ctx = timesc.Context(local)
+    stream = torch.cuda.current_stream()
+    x = torch.from_numpy(data).cuda()
+    ctx.znorm(x, ddof=1)
+    labels = torch.zeros(n, dtype=torch.int32, device="cuda")
+    ctx.init_labels(labels, k)
+    old = labels.clone()
+    C = torch.zeros((k, m), dtype=torch.float32, device="cuda")
+    shift = torch.zeros(n, dtype=torch.int32, device="cuda")
+    dist_b = torch.zeros(n, dtype=torch.float32, device="cuda")
+    changed = torch.zeros(1, dtype=torch.int32, device="cuda")
+    dsum = torch.zeros(1, dtype=torch.float64, device="cuda")
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+
+    def iteration(rec=None):
+        ctx.extract_shapes(x, labels, C, shift=shift, mode=mode, precision=prec)
+        changed.zero_()
+        dsum.zero_()
+        if rec:
+            rec[0].record(stream)
+        ctx.sbd_assign(x, C, mode=mode, precision=prec, labels=labels, dist=dist_b, shift=shift,
+                       old_labels=old, changed=changed, dist_sum=dsum)
+        if rec:
+            rec[1].record(stream)
+        return changed.item(), dsum.item()  # the reference reads its convergence flag back every iteration
+
+    for _ in range(args.warmup):
+        iteration()
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    clk = Clocks(local)
+    torch.cuda.synchronize()
+    l0 = timesc.lib().tc_launch_count()
+    t_start = torch.cuda.Event(enable_timing=True)
+    t_end = torch.cuda.Event(enable_timing=True)
+    t_start.record(stream)
+    for s in range(args.steps):
+        iteration(ev[s])
+    t_end.record(stream)
+    torch.cuda.synchronize()
+    launches = timesc.lib().tc_launch_count() - l0
+    clocks = clk.stop()
+    ms = t_start.elapsed_time(t_end)
+    assign_ms = [a.elapsed_time(b) for a, b in ev]
+    if dist:
+        t = torch.tensor([ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = t.item()
+        if dist:
+            dist.barrier()
+    ms_step = ms / args.steps
+    value = world * n * k / (ms_step / 1e3)
+    a_ms = statistics.mean(assign_ms)
+
+    out = None
+    if rank == 0:
+        hbm, bf16, peak_kind = load_peaks()
+        flops = fft_flops(n, k, F)
+        nbytes = assign_bytes(n, m, k)
+        achieved_gbs = nbytes / (a_ms / 1e3) / 1e9
+        sm_mhz = clocks.get("sm_mhz") or 2070.0
+        fp32_peak = 152 * 128 * 2 * sm_mhz * 1e6 / 1e12
+        roof = {"kernel": "k_assign_fft (fused SBD assignment, SIMT FP32)", "bound": "hbm",
+                "achieved": achieved_gbs, "peak": hbm, "unit": "GB/s", "frac": achieved_gbs / hbm,
+                "traffic": profiled_traffic(args.workload, args.mode, args.precision),
+                "peak_source": peak_kind,
+                "algorithmic_bytes_per_launch": nbytes, "launch_ms": a_ms,
+                "fp32_simt": {"achieved_tflops": flops / (a_ms / 1e3) / 1e12, "peak_tflops_at_median_clock":
+                              fp32_peak, "frac": flops / (a_ms / 1e3) / 1e12 / fp32_peak,
+                              "algorithmic_flops_per_launch": flops},
+                "note": "the FFT-form assignment is FP32-compute bound (about 475 flop/B); the HBM fraction is "
+                        "reported as the schema asks and the FP32 fraction beside it"}
+        out = {"metric": "SBD pairs/s (whole k-Shape iterations)", "value": value, "unit": "pairs/s",
+               "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_step,
+               "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+               "data": "synthetic (prototype generator: sinusoids + bump, shifted/scaled/offset, noise)",
+               "config": {"workload": desc, "mode": args.mode, "precision": args.precision, "fft_length": F,
+                          "parallelism": "replicas" if world > 1 else "single GPU",
+                          "l2": "inputs larger than L2 (%.1f GB of series)" % (4 * n * m / 1e9)},
+               "kshape_iters_per_s": 1e3 / ms_step,
+               "assign_pairs_per_s": n * k / (a_ms / 1e3),
+               "roofline": roof, "gpu_launches": int(launches), "clocks": clocks}
+
+    # end-to-end through the public C ABI with pinned host buffers
+    if not args.no_e2e:
+        pinned = torch.empty((n, m), dtype=torch.float32, pin_memory=True)
+        pinned.numpy()[:] = data
+        e_iters = 3
+        ctx.kshape_run(pinned.numpy(), k, mode=mode, precision=prec, max_iter=1, restart=False)  # warm
+        t0 = time.perf_counter()
+        r = ctx.kshape_run(pinned.numpy(), k, mode=mode, precision=prec, max_iter=e_iters, restart=False)
+        wall = time.perf_counter() - t0
+        if out is not None:
+            out["e2e"] = {"value": world * n * k * r["iterations"] / wall, "unit": "pairs/s",
+                          "h2d_bytes_per_step": 4 * n * m, "d2h_bytes_per_step": 4 * n + 4 * k * m,
+                          "iterations": r["iterations"], "wall_s": wall,
+                          "call": "tc_kshape_run(h_data pinned, max_iter=%d, restart=0)" % e_iters}
+    if out is not None and not args.no_cpu:
+        from oracle import oracle as O
+        X = O.znorm(data[:100_000].astype(np.float64))
+        lab_h = labels[:100_000].cpu().numpy()
+        C_h = C.cpu().numpy().astype(np.float64)
+        ns, dt, t_full = cpu_sample_iteration(O, X, C_h, lab_h, mode, F, target_s=10.0, n_full=n)
+        out["cpu_baseline"] = {"value": n * k / t_full, "unit": "pairs/s", "cores": host_threads(), "kind": "port",
+                               "sample": "one extract+assign iteration of the FP64 oracle on %d and %d of the %d "
+                                         "series (all %d centroids), extrapolated to all series; %.1f s measured"
+                                         % (ns, ns // 2, n, k, dt)}
+    if out is not None:
+        print(json.dumps(out))
+    ctx.close()
+    if dist:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -64,6 +64,9 @@ int tc_create(int device, tc_ctx** out);
 int tc_destroy(tc_ctx* ctx);
 /* Message of the last failed call on this context ("" if none). */
 const char* tc_last_error(const tc_ctx* ctx);
+/* Number of kernel launches this library has issued in this process (all
+ * contexts); for accounting in benchmarks.  No reference counterpart. */
+uint64_t tc_launch_count(void);
 
 /* ---------------------------------------------------------------- stages (device pointers) */
 /* FFT length the mode uses for series length m. */

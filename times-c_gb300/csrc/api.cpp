@@ -9,6 +9,8 @@
 
 namespace tc {
 
+std::atomic<uint64_t> g_launches{0};
+
 // ncc.cuh:12-16 and :473: 1 << (int)ceil(my_log2(2m-1)) with my_log2 returning a
 // truncated int, i.e. the largest power of two <= 2m-1.  Canonical k-Shape pads to
 // 1 << bit_length(2m-1) (test_timesC.py:88), a power of two >= 2m-1.
@@ -252,6 +254,8 @@ int tc_destroy(tc_ctx* ctx) {
 }
 
 const char* tc_last_error(const tc_ctx* ctx) { return ctx ? ctx->last_error.c_str() : "null context"; }
+
+uint64_t tc_launch_count(void) { return g_launches.load(); }
 
 int tc_fft_size(int m, int mode) {
     if (m < 1) return 0;

@@ -3,6 +3,7 @@
 
 #include <cuda_runtime.h>
 
+#include <atomic>
 #include <cstdint>
 #include <cstdio>
 #include <string>
@@ -23,7 +24,14 @@ struct TcError {
             throw TcError{TC_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_)}; \
     } while (0)
 
-#define TC_CHECK_LAUNCH() TC_CUDA(cudaGetLastError())
+namespace tc {
+extern std::atomic<uint64_t> g_launches;  // kernel launches issued by this library
+}
+#define TC_CHECK_LAUNCH()                 \
+    do {                                  \
+        ::tc::g_launches.fetch_add(1);    \
+        TC_CUDA(cudaGetLastError());      \
+    } while (0)
 
 #define TC_REQUIRE(cond, code, text)                         \
     do {                                                     \

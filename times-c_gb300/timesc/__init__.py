@@ -52,6 +52,7 @@ SIGNATURES = {
     "tc_create": (_int, [_int, ctypes.POINTER(_vp)]),
     "tc_destroy": (_int, [_vp]),
     "tc_last_error": (ctypes.c_char_p, [_vp]),
+    "tc_launch_count": (ctypes.c_uint64, []),
     "tc_fft_size": (_int, [_int, _int]),
     "tc_znorm": (_int, [_vp, _vp, _i64, _int, _int, _vp]),
     "tc_init_labels": (_int, [_vp, _vp, _i64, _int, _vp]),
