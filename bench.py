@@ -233,19 +233,18 @@ def main():
     ctx.init_labels(labels, k)
     old = labels.clone()
     C = torch.zeros((k, m), dtype=torch.float32, device="cuda")
-    shift = torch.zeros(n, dtype=torch.int32, device="cuda")
     dist_b = torch.zeros(n, dtype=torch.float32, device="cuda")
     changed = torch.zeros(1, dtype=torch.int32, device="cuda")
     dsum = torch.zeros(1, dtype=torch.float64, device="cuda")
     ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
 
     def iteration(rec=None):
-        ctx.extract_shapes(x, labels, C, shift=shift, mode=mode, precision=prec)
+        ctx.extract_shapes(x, labels, C, mode=mode, precision=prec)
         changed.zero_()
         dsum.zero_()
         if rec:
             rec[0].record(stream)
-        ctx.sbd_assign(x, C, mode=mode, precision=prec, labels=labels, dist=dist_b, shift=shift,
+        ctx.sbd_assign(x, C, mode=mode, precision=prec, labels=labels, dist=dist_b,
                        old_labels=old, changed=changed, dist_sum=dsum)
         if rec:
             rec[1].record(stream)

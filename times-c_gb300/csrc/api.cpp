@@ -85,7 +85,6 @@ static LoopState run_loop(tc_ctx* ctx, const tc_job* job, const float* x, int k,
     const int m = job->m;
     int32_t* labels = ws.labels.as<int32_t>(n);
     int32_t* old = ws.old_labels.as<int32_t>(n);
-    int32_t* shift = ws.shift.as<int32_t>(n);
     float* dist = ws.dist.as<float>(n);
     float* C = ws.centroids.as<float>((size_t)k * m);
     char* aux = ws.aux.as<char>(64);
@@ -124,7 +123,8 @@ static LoopState run_loop(tc_ctx* ctx, const tc_job* job, const float* x, int k,
     } h;
     auto do_assign = [&]() -> bool {
         TC_CUDA(cudaMemsetAsync(aux, 0, 16, s));
-        assign(ctx, x, C, n, m, k, job->mode, job->precision, labels, dist, shift, old, changed, dsum, s);
+        // no shifts here: an extraction whose gate opens computes them itself
+        assign(ctx, x, C, n, m, k, job->mode, job->precision, labels, dist, nullptr, old, changed, dsum, s);
         TC_CUDA(cudaMemcpyAsync(&h, aux, 16, cudaMemcpyDeviceToHost, s));
         TC_CUDA(cudaStreamSynchronize(s));
         st.inertia = h.dsum / (double)n;
@@ -148,7 +148,7 @@ static LoopState run_loop(tc_ctx* ctx, const tc_job* job, const float* x, int k,
         ExtractArgs e{};
         e.x = x;
         e.labels = labels;
-        e.shift = shift;
+        e.shift = nullptr;
         e.C = C;
         e.n = n;
         e.m = m;
@@ -160,12 +160,8 @@ static LoopState run_loop(tc_ctx* ctx, const tc_job* job, const float* x, int k,
         int sc = run_extract(ctx, e, s);
         if (!cal_select) st.sum_class = sc;  // get_class_centers_a leaves sum_class alone
     };
-    bool first_extract = true;
     for (int i = 0; i < cap; ++i) {
         if (!order_tsl) {
-            // at i = 0 the centroids are zero, so no gate opens and no shift is read
-            if (first_extract) TC_CUDA(cudaMemsetAsync(shift, 0, sizeof(int32_t) * n, s));
-            first_extract = false;
             extract();
             if (st.sum_class == 1 || st.sum_class <= k / 2) {
                 st.iterations = i + 1;

@@ -117,13 +117,14 @@ __device__ __forceinline__ void run_passes(float2* buf, int tid, int team, const
         team_sync<C::T>(team);
     } else {
         st.template compute<INV>(tid, twN);
-        st.each_output(tid, out);
+        out(st, tid);
     }
     if constexpr (!last) run_passes<N, PS + 1, INV, STORE_LAST>(buf, tid, team, twN, out);
 }
 
 struct NoOut {
-    __device__ void operator()(int, float2) const {}
+    template <class P>
+    __device__ void operator()(const P&, int) const {}
 };
 
 // Forward transform of one row into the thread's spectrum registers.
@@ -198,16 +199,34 @@ struct AssignParams {
     double* dist_sum;
 };
 
+// Max NCC over the valid lags with the lag of the first maximum in sbd3D's order
+// (needed for alignment shifts).
 struct LagOut {
     LagMax lm;
     int m, F;
-    __device__ void operator()(int o, float2 v) {
-        lag_take(lm, 2 * o, v.x, m, F);
-        lag_take(lm, 2 * o + 1, v.y, m, F);
+    template <class P>
+    __device__ void operator()(const P& st, int tid) {
+        st.each_output(tid, [this](int o, float2 v) {
+            lag_take(lm, 2 * o, v.x, m, F);
+            lag_take(lm, 2 * o + 1, v.y, m, F);
+        });
     }
 };
 
-template <int N, bool CSMEM>
+// Max NCC only: the thread's valid outputs are a fixed bit mask of its slots.
+struct MaxOut {
+    float val;
+    unsigned mask;
+    template <class P>
+    __device__ void operator()(const P& st, int tid) {
+        st.each_output_slot(tid, [this](int e, float2 v) {
+            if (mask & (1u << (2 * e))) val = fmaxf(val, v.x);
+            if (mask & (2u << (2 * e))) val = fmaxf(val, v.y);
+        });
+    }
+};
+
+template <int N, bool CSMEM, bool SHIFT>
 __global__ void __launch_bounds__(Cfg<N>::BLOCK, 1) k_assign_fft(AssignParams p) {
     typedef Core<N> Co;
     constexpr int T = Co::T, TEAMS = Cfg<N>::TEAMS;
@@ -225,6 +244,7 @@ __global__ void __launch_bounds__(Cfg<N>::BLOCK, 1) k_assign_fft(AssignParams p)
         __syncthreads();
     }
 
+    const unsigned vmask = Co::template Pass<Plan<N>::NPASS - 1>::valid_mask(tid, p.m, p.F);
     double dsum = 0.0;
     int nchg = 0;
     const int64_t stride = (int64_t)gridDim.x * TEAMS;
@@ -251,12 +271,23 @@ __global__ void __launch_bounds__(Cfg<N>::BLOCK, 1) k_assign_fft(AssignParams p)
             }
             Co::template pass0_store<true>(v, tid, buf);
             team_sync<T>(team);
-            LagOut out;
-            out.lm.init();
-            out.m = p.m;
-            out.F = p.F;
-            run_passes<N, 1, true, false>(buf, tid, team, p.twN, out);
-            LagMax lm = team_max<T>(out.lm, team, tid, scr);
+            LagMax lm;
+            if constexpr (SHIFT) {
+                LagOut out;
+                out.lm.init();
+                out.m = p.m;
+                out.F = p.F;
+                run_passes<N, 1, true, false>(buf, tid, team, p.twN, out);
+                lm = team_max<T>(out.lm, team, tid, scr);
+            } else {
+                MaxOut out;
+                out.val = -3.0e38f;
+                out.mask = vmask;
+                run_passes<N, 1, true, false>(buf, tid, team, p.twN, out);
+                lm.val = out.val;
+                lm.u = 0;
+                lm = team_max<T>(lm, team, tid, scr);
+            }
             team_sync<T>(team);
             if (tid == 0) {
                 float d = 1.0f - lm.val;
@@ -292,6 +323,17 @@ static void centroid_spectra_n(tc_ctx* ctx, const float* C, int k, int m, float2
     TC_CHECK_LAUNCH();
 }
 
+template <int N, bool CSMEM, bool SHIFT>
+static void launch_variant(tc_ctx* ctx, const AssignParams& p, size_t sm, cudaStream_t s) {
+    auto fn = k_assign_fft<N, CSMEM, SHIFT>;
+    TC_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+    int per_sm = 0;
+    TC_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, Cfg<N>::BLOCK, sm));
+    const int64_t teams_needed = (p.n + Cfg<N>::TEAMS - 1) / Cfg<N>::TEAMS;
+    const int grid = (int)std::min<int64_t>(teams_needed, (int64_t)ctx->sm_count * std::max(per_sm, 1));
+    fn<<<grid, Cfg<N>::BLOCK, sm, s>>>(p);
+}
+
 template <int N>
 static void assign_n(tc_ctx* ctx, const AssignArgs& a, cudaStream_t s) {
     const FftTables& tb = fft_tables(ctx, 2 * N);
@@ -314,20 +356,13 @@ static void assign_n(tc_ctx* ctx, const AssignArgs& a, cudaStream_t s) {
     p.dist_sum = a.dist_sum;
     bool csmem = Cfg<N>::smem(a.k, true) <= ctx->smem_optin;
     size_t sm = Cfg<N>::smem(a.k, csmem);
-    int64_t teams_needed = (a.n + Cfg<N>::TEAMS - 1) / Cfg<N>::TEAMS;
-    int grid;
+    const bool want_shift = a.shift != nullptr || a.fixed != nullptr;
     if (csmem) {
-        TC_CUDA(cudaFuncSetAttribute(k_assign_fft<N, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
-        int per_sm = 0;
-        TC_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_assign_fft<N, true>, Cfg<N>::BLOCK, sm));
-        grid = (int)std::min<int64_t>(teams_needed, (int64_t)ctx->sm_count * std::max(per_sm, 1));
-        k_assign_fft<N, true><<<grid, Cfg<N>::BLOCK, sm, s>>>(p);
+        if (want_shift) launch_variant<N, true, true>(ctx, p, sm, s);
+        else launch_variant<N, true, false>(ctx, p, sm, s);
     } else {
-        TC_CUDA(cudaFuncSetAttribute(k_assign_fft<N, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
-        int per_sm = 0;
-        TC_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_assign_fft<N, false>, Cfg<N>::BLOCK, sm));
-        grid = (int)std::min<int64_t>(teams_needed, (int64_t)ctx->sm_count * std::max(per_sm, 1));
-        k_assign_fft<N, false><<<grid, Cfg<N>::BLOCK, sm, s>>>(p);
+        if (want_shift) launch_variant<N, false, true>(ctx, p, sm, s);
+        else launch_variant<N, false, false>(ctx, p, sm, s);
     }
     TC_CHECK_LAUNCH();
 }

@@ -114,6 +114,35 @@ struct Core {
                 }
             }
         }
+        // outputs with their slot e = b*R + q in this thread (constant after unrolling)
+        template <class F>
+        TC_HD void each_output_slot(int tid, F&& fn) const {
+#pragma unroll
+            for (int b = 0; b < PER; ++b) {
+                if (tid + b * T < NB) {
+#pragma unroll
+                    for (int q = 0; q < R; ++q) fn(b * R + q, v[b][q]);
+                }
+            }
+        }
+        // bit 2e / 2e+1: the two real outputs of slot e are valid lags (t <= m-1 or
+        // t >= F-m+1) of an existing butterfly.  Every plan has PER*R <= 16.
+        TC_HD static unsigned valid_mask(int tid, int m, int F) {
+            unsigned mask = 0;
+#pragma unroll
+            for (int b = 0; b < PER; ++b) {
+                const int j = tid + b * T;
+#pragma unroll
+                for (int q = 0; q < R; ++q) {
+                    const int t = 2 * out_index(j, q, NS, R);
+                    const bool ok = j < NB;
+                    const unsigned b0 = (ok && (t <= m - 1 || t >= F - m + 1)) ? 1u : 0u;
+                    const unsigned b1 = (ok && (t + 1 <= m - 1 || t + 1 >= F - m + 1)) ? 2u : 0u;
+                    mask |= (b0 | b1) << (2 * (b * R + q));
+                }
+            }
+            return mask;
+        }
     };
 
     // Real-to-complex post-processing of the forward transform (natural-order Z in
