@@ -140,6 +140,24 @@ def test_extract_shapes(gpu_ctx, mods, mode, m, k, n, cinit):
     assert err.max() < 1e-4, err
 
 
+@pytest.mark.parametrize("prec,tol", [(2, 2e-3), (1, 1e-2)])
+@pytest.mark.parametrize("m,k,n", [(128, 4, 700), (300, 3, 500), (512, 8, 3000), (1000, 2, 200)])
+def test_extract_tensor_core_gram(gpu_ctx, mods, prec, tol, m, k, n):
+    """Mixed-precision extraction: TF32 (prec 2) / BF16 (prec 1) Gram on tcgen05."""
+    import torch
+    T, O = mods
+    data, truth = make_data(T, n, m, k, seed=3 * m + k)
+    X = O.znorm(data.astype(np.float64)).astype(np.float32)
+    C = np.zeros((k, m), np.float32)
+    x, lab, c = dev(X), dev(truth), dev(C)
+    sc = gpu_ctx.extract_shapes(x, lab, c, mode=0, precision=prec)
+    torch.cuda.synchronize()
+    refC, _, refsc = O.extract(X.astype(np.float64), truth, C.astype(np.float64), 0)
+    assert sc == refsc
+    err = np.abs(c.cpu().numpy() - refC).max()
+    assert err < tol, err
+
+
 def _cpu_labels_via_gpu_init(ctx, n, k):
     import torch
     t = torch.zeros(n, dtype=torch.int32, device="cuda")

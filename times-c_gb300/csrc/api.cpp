@@ -236,7 +236,7 @@ int tc_destroy(tc_ctx* ctx) {
     DevBuf* bufs[] = {&ctx->ws.x, &ctx->ws.labels, &ctx->ws.old_labels, &ctx->ws.shift, &ctx->ws.dist,
                       &ctx->ws.centroids, &ctx->ws.spectra, &ctx->ws.seg, &ctx->ws.perm, &ctx->ws.chunk_counts,
                       &ctx->ws.counts, &ctx->ws.offsets, &ctx->ws.gate, &ctx->ws.scal, &ctx->ws.gram,
-                      &ctx->ws.rowsum, &ctx->ws.piter, &ctx->ws.pstats, &ctx->ws.aux, &ctx->ws.toeplitz,
+                      &ctx->ws.rowsum, &ctx->ws.gram_yt, &ctx->ws.gram_poff, &ctx->ws.piter, &ctx->ws.pstats, &ctx->ws.aux, &ctx->ws.toeplitz,
                       &ctx->ws.xbf};
     for (DevBuf* b : bufs) b->release();
     for (auto* t : ctx->fft) {

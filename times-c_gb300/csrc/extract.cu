@@ -25,8 +25,9 @@ namespace tc {
 void launch_gather_norm(const float* x, const int32_t* perm, const int32_t* labels, const int32_t* shift,
                         const uint8_t* gate, int64_t n, int m, float* seg, int sm_count, cudaStream_t s);
 bool gram_tc_supported(int m, int precision);
-void launch_gram_tc(tc_ctx* ctx, const float* seg, const int32_t* counts, const int32_t* offsets, int k, int m,
-                    int precision, float* S, cudaStream_t s);
+void launch_gram_tc(tc_ctx* ctx, const float* seg, const int32_t* counts, const int32_t* offsets,
+                    const std::vector<int32_t>& h_counts, int64_t n, int k, int m, int precision, float* S,
+                    cudaStream_t s);
 
 constexpr int SEG_CHUNK = 4096;
 constexpr int SEG_BLOCK = 256;
@@ -440,15 +441,19 @@ __global__ void __launch_bounds__(1024, 1) k_power_persistent(PowerParams p) {
             if (p.counts[c] != 0) atomicAdd(pst(p.st, k, t + 1, c) + q, sum);
         }
         grid_barrier(p.bar, G, gen, p.status);
+        // every block reads the same published step differences (in parallel)
+        double mx = 0;
+        if (t >= 1)
+            for (int c = threadIdx.x; c < k; c += blockDim.x)
+                if (p.counts[c] != 0) mx = fmax(mx, __ldcg(pst(p.st, k, t + 1, c) + 3));
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+        if (lane == 0) wacc[wid][0][0] = mx;
+        __syncthreads();
         if (threadIdx.x == 0) {
-            bool done = t >= p.tmax || __ldcg(p.status) != 0;
-            if (!done && t >= 1) {
-                double mx = 0;
-                for (int c = 0; c < k; ++c)
-                    if (p.counts[c] != 0) mx = fmax(mx, __ldcg(pst(p.st, k, t + 1, c) + 3));
-                done = mx < p.tol2;
-            }
-            sh_done = done;
+            double all = 0;
+            for (int w = 0; w < nw; ++w) all = fmax(all, wacc[w][0][0]);
+            sh_done = t >= p.tmax || __ldcg(p.status) != 0 || (t >= 1 && all < p.tol2);
         }
         __syncthreads();
         if (sh_done) {
@@ -638,7 +643,7 @@ int run_extract(tc_ctx* ctx, const ExtractArgs& a, cudaStream_t s) {
     // Gram
     const int nt = ceil_div(m, 64);
     if (gram_tc_supported(m, a.precision)) {
-        launch_gram_tc(ctx, seg, counts, offsets, k, m, a.precision, S, s);
+        launch_gram_tc(ctx, seg, counts, offsets, h_counts, n, k, m, a.precision, S, s);
     } else {
         dim3 g(nt * (nt + 1) / 2, k);
         k_gram_simt<<<g, 256, 0, s>>>(seg, counts, offsets, m, nt, S);

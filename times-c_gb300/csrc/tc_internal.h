@@ -81,6 +81,8 @@ struct Workspace {
     DevBuf seg;          // aligned, re-normalised members in cluster order, n*m (f32 or bf16)
     DevBuf perm, chunk_counts, counts, offsets, gate, scal;
     DevBuf gram;         // k*m*m f32
+    DevBuf gram_yt;      // transposed, cluster-padded members for the tensor-core Gram
+    DevBuf gram_poff;    // padded cluster offsets (int64)
     DevBuf rowsum;       // k*m f64 + k f64
     DevBuf piter;        // power-iteration vectors 3*k*m f32
     DevBuf pstats;       // 3*k*4 f64

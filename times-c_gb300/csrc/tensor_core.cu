@@ -1,12 +1,266 @@
-// Tensor-core (tcgen05) paths: Gram matrices and the BF16/TF32 correlation.
+// Tensor-core (tcgen05) Gram matrices for the mixed-precision extraction, and
+// (not yet built) the tensor-core correlation.
+//
+// S_c = Y_c^T Y_c (shapeExtract.cuh:532-537, a cuBLAS SGEMM per cluster with
+// k CUDA streams in the reference) becomes one launch over all clusters and the
+// 128x128 upper-triangle tiles of every S_c:
+//   * the aligned members are transposed into YT[a][p'] (BF16, or FP32 rounded
+//     to TF32) with each cluster's positions padded to a multiple of 64, so a
+//     cluster is a contiguous, 128-byte aligned K range;
+//   * per CTA a TMA producer thread streams 128-row x 128-byte K-major tiles of
+//     YT (rows a0.. and b0..) through a 4-stage mbarrier pipeline with the
+//     128-byte swizzle; one thread issues tcgen05.mma (M=128, N=128) into a
+//     128-column FP32 TMEM accumulator;
+//   * four warps read TMEM back (tcgen05.ld 32x32b) and write the tile and its
+//     mirror image.
+// All waits are bounded and report through an error word.
+#include <cuda.h>
+#include <cuda_bf16.h>
+
+#include <algorithm>
+#include <vector>
+
+#include "sm100.cuh"
 #include "tc_internal.h"
 
 namespace tc {
 
-bool gram_tc_supported(int, int) { return false; }
-void launch_gram_tc(tc_ctx*, const float*, const int32_t*, const int32_t*, int, int, int, float*, cudaStream_t) {
-    throw TcError{TC_ERR_UNSUPPORTED, "tensor-core Gram not built"};
+constexpr int GT_STAGES = 4;
+constexpr int GT_TILE = 128;                       // rows per operand tile
+constexpr int GT_TILE_BYTES = GT_TILE * 128;       // 128 rows x 128 bytes
+constexpr int GT_SMEM = GT_STAGES * 2 * GT_TILE_BYTES + 1024;  // + alignment slack
+constexpr int GT_PAD = 64;                          // cluster K padding (elements)
+
+// ---------------------------------------------------------------- TMA descriptor
+typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+                                   const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
+                                   CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+static EncodeTiledFn encode_fn() {
+    static EncodeTiledFn fn = nullptr;
+    if (!fn) {
+        void* p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        TC_CUDA(cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q));
+        TC_REQUIRE(q == cudaDriverEntryPointSuccess && p, TC_ERR_CUDA, "cuTensorMapEncodeTiled unavailable");
+        fn = reinterpret_cast<EncodeTiledFn>(p);
+    }
+    return fn;
 }
+
+// 2-D row-major tensor [rows][cols] of esize-byte elements; box = 128 bytes x box_rows.
+static CUtensorMap make_tmap_2d(const void* base, CUtensorMapDataType dt, int esize, uint64_t rows, uint64_t cols,
+                                uint32_t box_rows) {
+    CUtensorMap map;
+    cuuint64_t dims[2] = {cols, rows};
+    cuuint64_t strides[1] = {cols * (uint64_t)esize};
+    cuuint32_t box[2] = {(cuuint32_t)(128 / esize), box_rows};
+    cuuint32_t estr[2] = {1, 1};
+    CUresult r = encode_fn()(&map, dt, 2, const_cast<void*>(base), dims, strides, box, estr,
+                             CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+                             CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    TC_REQUIRE(r == CUDA_SUCCESS, TC_ERR_CUDA, "cuTensorMapEncodeTiled failed (" + std::to_string((int)r) + ")");
+    return map;
+}
+
+// ---------------------------------------------------------------- transpose
+__device__ __forceinline__ float to_tf32(float x) {
+    uint32_t r;
+    asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(r) : "f"(x));
+    return __uint_as_float(r);
+}
+template <class TO>
+__device__ __forceinline__ TO convert_out(float v);
+template <>
+__device__ __forceinline__ __nv_bfloat16 convert_out<__nv_bfloat16>(float v) { return __float2bfloat16_rn(v); }
+template <>
+__device__ __forceinline__ float convert_out<float>(float v) { return to_tf32(v); }
+
+// YT[a][p'] = seg[pos][a], p' = pos - offsets[c] + poff[c] for the cluster c holding pos.
+template <class TO>
+__global__ void k_seg_transpose(const float* __restrict__ seg, int64_t n, int m, const int32_t* __restrict__ offsets,
+                                const int32_t* __restrict__ counts, const int64_t* __restrict__ poff, int k,
+                                TO* __restrict__ YT, int64_t Pp) {
+    __shared__ float tile[32][33];
+    const int tx = threadIdx.x, ty = threadIdx.y;
+    const int64_t pos0 = (int64_t)blockIdx.x * 32;
+    const int a0 = blockIdx.y * 32;
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+        const int64_t pos = pos0 + ty + 8 * i;
+        const int a = a0 + tx;
+        tile[ty + 8 * i][tx] = (pos < n && a < m) ? seg[pos * m + a] : 0.f;
+    }
+    __syncthreads();
+    const int64_t pos = pos0 + tx;
+    if (pos >= n) return;
+    int lo = 0, hi = k - 1;  // last cluster whose offset <= pos (non-empty)
+    while (lo < hi) {
+        int mid = (lo + hi + 1) >> 1;
+        if (offsets[mid] <= pos) lo = mid;
+        else hi = mid - 1;
+    }
+    while (counts[lo] == 0 && lo > 0) --lo;
+    const int64_t pp = pos - offsets[lo] + poff[lo];
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+        const int a = a0 + ty + 8 * i;
+        if (a < m) YT[(int64_t)a * Pp + pp] = convert_out<TO>(tile[tx][ty + 8 * i]);
+    }
+}
+
+// ---------------------------------------------------------------- Gram kernel
+template <int FMT>
+__global__ void __launch_bounds__(128, 1) k_gram_tc(const __grid_constant__ CUtensorMap tmap,
+                                                    const int32_t* __restrict__ counts,
+                                                    const int64_t* __restrict__ poff, int m, int nt,
+                                                    float* __restrict__ S, int* __restrict__ err) {
+    extern __shared__ uint8_t smem_raw[];
+    __shared__ __align__(8) uint64_t full[GT_STAGES], empty[GT_STAGES], done;
+    __shared__ uint32_t tmem_base;
+    uint8_t* base = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+    const int c = blockIdx.y;
+    const int cnt = counts[c];
+    if (cnt == 0) return;
+    int t = blockIdx.x, ta = 0;
+    while (t >= nt - ta) { t -= nt - ta; ++ta; }
+    const int tb = ta + t;
+    constexpr int KE = FMT == 2 ? 32 : 64;  // elements per 128-byte K slab
+    const int nk = (cnt + KE - 1) / KE;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    if (threadIdx.x == 0) {
+        for (int s = 0; s < GT_STAGES; ++s) {
+            sm100::mbar_init(&full[s], 1);
+            sm100::mbar_init(&empty[s], 1);
+        }
+        sm100::mbar_init(&done, 1);
+        sm100::fence_mbar_init();
+        sm100::prefetch_tmap(&tmap);
+    }
+    if (warp == 0) {
+        sm100::tmem_alloc(&tmem_base, 128);
+        sm100::tmem_relinquish();
+    }
+    sm100::tc_fence_before();
+    __syncthreads();
+    sm100::tc_fence_after();
+    const uint32_t tmem = tmem_base;
+    const int x0 = (int)poff[c];
+    bool ok = true;
+    if (warp == 0 && lane == 0) {
+        // TMA producer
+        for (int kb = 0; kb < nk && ok; ++kb) {
+            const int s = kb % GT_STAGES, u = kb / GT_STAGES;
+            if (u > 0) ok = sm100::mbar_wait(&empty[s], (u - 1) & 1, err);
+            if (!ok) break;
+            uint8_t* A = base + (size_t)s * 2 * GT_TILE_BYTES;
+            sm100::mbar_expect_tx(&full[s], 2 * GT_TILE_BYTES);
+            sm100::tma_load_2d(A, &tmap, x0 + kb * KE, ta * GT_TILE, &full[s]);
+            sm100::tma_load_2d(A + GT_TILE_BYTES, &tmap, x0 + kb * KE, tb * GT_TILE, &full[s]);
+        }
+    } else if (warp == 1 && lane == 0) {
+        // MMA issuer
+        constexpr uint32_t ID = sm100::idesc(FMT, 128, 128);
+        for (int kb = 0; kb < nk && ok; ++kb) {
+            const int s = kb % GT_STAGES, u = kb / GT_STAGES;
+            ok = sm100::mbar_wait(&full[s], u & 1, err);
+            if (!ok) break;
+            sm100::tc_fence_after();
+            uint8_t* A = base + (size_t)s * 2 * GT_TILE_BYTES;
+            const uint64_t da = sm100::desc_k_sw128(A), db = sm100::desc_k_sw128(A + GT_TILE_BYTES);
+#pragma unroll
+            for (int kk = 0; kk < 4; ++kk) {  // 4 x 32 bytes of K per slab
+                if (FMT == 2) sm100::mma_tf32(tmem, da + 2 * kk, db + 2 * kk, ID, (kb | kk) != 0);
+                else sm100::mma_f16(tmem, da + 2 * kk, db + 2 * kk, ID, (kb | kk) != 0);
+            }
+            sm100::mma_commit(&empty[s]);
+        }
+        sm100::mma_commit(&done);
+    }
+    __syncwarp();
+    // epilogue: warp w owns TMEM lanes 32w..32w+31 = rows a0 + 32w + lane
+    const bool fin = __syncthreads_and(sm100::mbar_wait(&done, 0, err)) != 0;
+    sm100::tc_fence_after();
+    if (fin) {
+        const int a = ta * GT_TILE + warp * 32 + lane;
+        float* Sc = S + (size_t)c * m * m;
+        for (int cb = 0; cb < 4; ++cb) {
+            float r[32];
+            sm100::tmem_ld32(tmem + ((uint32_t)(warp * 32) << 16) + cb * 32, r);
+            sm100::tmem_ld_wait();
+            const int b0 = tb * GT_TILE + cb * 32;
+            if (a < m) {
+#pragma unroll
+                for (int j = 0; j < 32; ++j)
+                    if (b0 + j < m) Sc[(size_t)a * m + b0 + j] = r[j];
+            }
+            if (ta != tb) {
+#pragma unroll
+                for (int j = 0; j < 32; ++j)
+                    if (b0 + j < m && a < m) Sc[(size_t)(b0 + j) * m + a] = r[j];
+            }
+        }
+    } else if (threadIdx.x == 0) {
+        // the pipeline stopped early: let copies already issued land before the CTA leaves
+        for (int s = 0; s < GT_STAGES; ++s) sm100::mbar_wait(&full[s], 0, nullptr);
+    }
+    sm100::tc_fence_before();
+    __syncthreads();
+    if (warp == 0) sm100::tmem_dealloc(tmem, 128);
+}
+
+// ---------------------------------------------------------------- host
+bool gram_tc_supported(int m, int precision) {
+    return (precision == TC_PREC_BF16 || precision == TC_PREC_TF32) && m >= 2;
+}
+
+void launch_gram_tc(tc_ctx* ctx, const float* seg, const int32_t* counts, const int32_t* offsets,
+                    const std::vector<int32_t>& h_counts, int64_t n, int k, int m, int precision, float* S,
+                    cudaStream_t s) {
+    Workspace& ws = ctx->ws;
+    std::vector<int64_t> hp(k);
+    int64_t Pp = 0;
+    for (int j = 0; j < k; ++j) {
+        hp[j] = Pp;
+        Pp += (h_counts[j] + GT_PAD - 1) / GT_PAD * GT_PAD;
+    }
+    Pp = std::max<int64_t>(Pp, GT_PAD);
+    int64_t* poff = ws.gram_poff.as<int64_t>(k);
+    TC_CUDA(cudaMemcpyAsync(poff, hp.data(), sizeof(int64_t) * k, cudaMemcpyHostToDevice, s));
+    const bool tf32 = precision == TC_PREC_TF32;
+    const int esize = tf32 ? 4 : 2;
+    void* YT = ws.gram_yt.get((size_t)m * Pp * esize);
+    TC_CUDA(cudaMemsetAsync(YT, 0, (size_t)m * Pp * esize, s));
+    dim3 tg(ceil_div(n, 32), ceil_div(m, 32)), tb(32, 8);
+    if (n > 0) {
+        if (tf32)
+            k_seg_transpose<float><<<tg, tb, 0, s>>>(seg, n, m, offsets, counts, poff, k, (float*)YT, Pp);
+        else
+            k_seg_transpose<__nv_bfloat16><<<tg, tb, 0, s>>>(seg, n, m, offsets, counts, poff, k,
+                                                             (__nv_bfloat16*)YT, Pp);
+        TC_CHECK_LAUNCH();
+    }
+    CUtensorMap map = make_tmap_2d(YT, tf32 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT32 : CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, esize,
+                                   (uint64_t)m, (uint64_t)Pp, GT_TILE);
+    int* err = reinterpret_cast<int*>(ws.aux.as<char>(64) + 48);
+    TC_CUDA(cudaMemsetAsync(err, 0, sizeof(int), s));
+    const int nt = ceil_div(m, GT_TILE);
+    dim3 grid(nt * (nt + 1) / 2, k);
+    if (tf32) {
+        TC_CUDA(cudaFuncSetAttribute(k_gram_tc<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, GT_SMEM));
+        k_gram_tc<2><<<grid, 128, GT_SMEM, s>>>(map, counts, poff, m, nt, S, err);
+    } else {
+        TC_CUDA(cudaFuncSetAttribute(k_gram_tc<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, GT_SMEM));
+        k_gram_tc<1><<<grid, 128, GT_SMEM, s>>>(map, counts, poff, m, nt, S, err);
+    }
+    TC_CHECK_LAUNCH();
+    int h_err = 0;
+    TC_CUDA(cudaMemcpyAsync(&h_err, err, sizeof(int), cudaMemcpyDeviceToHost, s));
+    TC_CUDA(cudaStreamSynchronize(s));
+    TC_REQUIRE(h_err == 0, TC_ERR_TIMEOUT, "tensor-core Gram: a pipeline wait ran out");
+}
+
+// ---------------------------------------------------------------- correlation (not built yet)
 bool tc_assign_supported(int, int, int, int) { return false; }
 void launch_assign_tc(tc_ctx*, const AssignArgs&, int, cudaStream_t) {
     throw TcError{TC_ERR_UNSUPPORTED, "tensor-core correlation not built"};
