@@ -44,6 +44,8 @@ WORKLOADS = {
     "c3": (1_000_000, 512, 32, 0.3, 0.0, "precision form: n=1e6 m=512 k=32, FP32 series, noise 0.3"),
     "c2": (20_000, 2709, 8, 0.2, 2.0, "at scale: n=2e4 m=2709 k=8, Dirichlet(2) classes"),
     "c1": (300, 128, 4, 0.2, 0.0, "CPU-runnable: n=300 m=128 k=4"),
+    # profiling case: the precision form with a tenth of the series (still larger than L2)
+    "c3s": (100_000, 512, 32, 0.3, 0.0, "profiling case: n=1e5 m=512 k=32, noise 0.3"),
 }
 PREC = {"fp32": 0, "bf16": 1, "tf32": 2}
 MODES = {"compat": 0, "canonical": 1}
