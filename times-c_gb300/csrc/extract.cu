@@ -11,7 +11,7 @@
 //   centring  M = Q S Q is never formed: M v = S v - (1.v/m) r - (r.v/m) 1
 //             + (tot 1.v/m^2) 1 with r = S 1, tot = 1^T S 1 (replaces get_matQ and
 //             two in-place m^3 GEMMs, :204-214, :551-570).
-//   power     all clusters advance together, one launch per step, with the
+//   power     power.cu: all clusters in one cooperative launch, with the
 //             Rayleigh quotient, the step difference and the norms in FP64
 //             (:269-360, :577-630); the sign rule and the store are fused into
 //             the final kernel (get_center, :217-264).
@@ -260,309 +260,9 @@ __global__ void k_rowsum(const float* __restrict__ S, const int32_t* __restrict_
     }
 }
 
-// ---------------------------------------------------------------- power iteration
-// Step t: v_t = u_t / |u_t|, u_{t+1} = M v_t.  u lives in 3 rotating slots of k*m
-// floats; per-step statistics in 4 rotating slots of k*4 doubles:
-//   st[slot][c] = { |u|^2, sum u, r.u, |v_t - v_{t-1}|^2 }  (slot of u_{t+1} holds delta_t).
-constexpr int PST = 4;
-
-__device__ __forceinline__ double* pst(double* st, int k, int t, int c) { return st + ((size_t)(t & 3) * k + c) * PST; }
-
-__global__ void k_power_prep(const int32_t* __restrict__ counts, const double* __restrict__ r, int k, int m,
-                             float* __restrict__ u, double* __restrict__ st) {
-    __shared__ double red[32];
-    const int c = blockIdx.x;
-    double s = 0, sy = 0, ry = 0;
-    for (int a = threadIdx.x; a < m; a += blockDim.x) {
-        float v = (a % 2 == 0) ? 1.0f : 0.5f;  // init_vec (shapeExtract.cuh:269-283)
-        u[(size_t)c * m + a] = v;
-        s += (double)v * v;
-        sy += v;
-        ry += r[(size_t)c * m + a] * (double)v;
-    }
-    s = block_sum_d(s, red);
-    sy = block_sum_d(sy, red);
-    ry = block_sum_d(ry, red);
-    if (threadIdx.x < 4 * PST) {
-        int slot = threadIdx.x / PST, q = threadIdx.x % PST;
-        double v = 0;
-        if (slot == 0) v = q == 0 ? s : (q == 1 ? sy : (q == 2 ? ry : 0.0));
-        st[((size_t)slot * k + c) * PST + q] = v;
-    }
-    (void)counts;
-}
-
-struct PowerParams {
-    const float* S;
-    const double* r;
-    const double* tot;
-    const int32_t* counts;
-    int k, m, tmax;
-    double tol2;
-    float* u;
-    double* st;
-    unsigned* bar;  // [0] arrivals, [1] generation
-    int* status;    // [0] barrier timeout, [1] final T
-};
-
-constexpr unsigned long long BAR_SPIN_LIMIT = 1ull << 22;
-
-// Grid-wide barrier of a cooperative launch (all blocks co-resident).  The wait is
-// bounded: after BAR_SPIN_LIMIT polls it records a timeout in *err and returns,
-// so a fault elsewhere can never hang the GPU here.
-__device__ __forceinline__ void grid_barrier(unsigned* bar, unsigned nblocks, unsigned& gen, int* err) {
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        __threadfence();
-        unsigned arrived = atomicAdd(&bar[0], 1u);
-        if (arrived == nblocks - 1) {
-            atomicExch(&bar[0], 0u);
-            __threadfence();
-            atomicAdd(&bar[1], 1u);
-        } else {
-            unsigned long long spins = 0;
-            while (*(volatile unsigned*)&bar[1] == gen) {
-                __nanosleep(64);
-                if (++spins > BAR_SPIN_LIMIT) {
-                    atomicExch(err, 1);
-                    break;
-                }
-            }
-        }
-        ++gen;
-        __threadfence();
-    }
-    __syncthreads();
-}
-
-// All clusters' power iterations in one cooperative launch.  Block b owns the
-// contiguous rows [b*R/G, (b+1)*R/G) of the stacked k*m row space (so it touches
-// at most a few clusters); each warp computes whole rows of S v from L2/HBM with
-// v in shared memory.  After each step a grid barrier publishes u_{t+1} and the
-// FP64 statistics; every block then reads the same step differences and leaves
-// the loop at the same t: when every non-empty cluster moved less than tol, or
-// at t = tmax.
-__global__ void __launch_bounds__(1024, 1) k_power_persistent(PowerParams p) {
-    extern __shared__ float sm_v[];  // ncl * m
-    __shared__ double wacc[32][8][PST];  // per warp, per local cluster (no atomics)
-    __shared__ double sh_corr[8][3];     // per local cluster: corr_r, corr_const, inv_prev
-    __shared__ int sh_done;
-    const int k = p.k, m = p.m;
-    const int64_t R = (int64_t)k * m;
-    const unsigned G = gridDim.x;
-    const int64_t r0 = R * blockIdx.x / G, r1 = R * (blockIdx.x + 1) / G;
-    const int c_lo = (int)(r0 / m);
-    const int ncl = r1 > r0 ? (int)((r1 - 1) / m) - c_lo + 1 : 0;
-    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
-    unsigned gen = 0;
-    for (int t = 0;; ++t) {
-        const int uc = t % 3, un = (t + 1) % 3, up = (t + 2) % 3;
-        if (blockIdx.x == 0)  // slot of step t+1's sums: last read at step t-1
-            for (int e = threadIdx.x; e < k * PST; e += blockDim.x) p.st[(size_t)((t + 2) & 3) * k * PST + e] = 0.0;
-        // v_t of the clusters this block touches, and the centring terms
-        for (int lc = 0; lc < ncl; ++lc) {
-            const int c = c_lo + lc;
-            if (p.counts[c] == 0) continue;
-            const double* sc = pst(p.st, k, t, c);
-            const double n2 = __ldcg(sc), inv = 1.0 / sqrt(n2);
-            const float finv = (float)inv;
-            const float* ucur = p.u + ((size_t)uc * k + c) * m;
-            for (int b = threadIdx.x; b < m; b += blockDim.x) sm_v[(size_t)lc * m + b] = __ldcg(ucur + b) * finv;
-            if (threadIdx.x == 0) {
-                const double sv = __ldcg(sc + 1) * inv, rv = __ldcg(sc + 2) * inv, mm = (double)m;
-                sh_corr[lc][0] = -sv / mm;
-                sh_corr[lc][1] = -rv / mm + p.tot[c] * sv / (mm * mm);
-                sh_corr[lc][2] = t >= 1 ? 1.0 / sqrt(__ldcg(pst(p.st, k, t - 1, c))) : 0.0;
-            }
-        }
-        for (int e = threadIdx.x; e < 32 * 8 * PST; e += blockDim.x) (&wacc[0][0][0])[e] = 0.0;
-        __syncthreads();
-        // rows (a warp's rows increase, so its cluster changes at most ncl-1 times)
-        double acc[PST] = {0.0, 0.0, 0.0, 0.0};
-        int acc_lc = -1;
-        for (int64_t row = r0 + wid; row < r1; row += nw) {
-            const int c = (int)(row / m), a = (int)(row % m), lc = c - c_lo;
-            if (p.counts[c] == 0) continue;
-            const float* Srow = p.S + (size_t)row * m;
-            const float* v = sm_v + (size_t)lc * m;
-            float s0 = 0.f, s1 = 0.f;
-            if ((m & 3) == 0) {
-                const float4* S4 = reinterpret_cast<const float4*>(Srow);
-                const float4* v4 = reinterpret_cast<const float4*>(v);
-                int b = lane;
-                for (; b + 32 < m / 4; b += 64) {
-                    float4 x0 = __ldg(S4 + b), x1 = __ldg(S4 + b + 32), w0 = v4[b], w1 = v4[b + 32];
-                    s0 = fmaf(x0.x, w0.x, s0); s0 = fmaf(x0.y, w0.y, s0); s0 = fmaf(x0.z, w0.z, s0); s0 = fmaf(x0.w, w0.w, s0);
-                    s1 = fmaf(x1.x, w1.x, s1); s1 = fmaf(x1.y, w1.y, s1); s1 = fmaf(x1.z, w1.z, s1); s1 = fmaf(x1.w, w1.w, s1);
-                }
-                for (; b < m / 4; b += 32) {
-                    float4 x0 = __ldg(S4 + b), w0 = v4[b];
-                    s0 = fmaf(x0.x, w0.x, s0); s0 = fmaf(x0.y, w0.y, s0); s0 = fmaf(x0.z, w0.z, s0); s0 = fmaf(x0.w, w0.w, s0);
-                }
-            } else {
-                int b = lane;
-                for (; b + 32 < m; b += 64) {
-                    s0 = fmaf(__ldg(Srow + b), v[b], s0);
-                    s1 = fmaf(__ldg(Srow + b + 32), v[b + 32], s1);
-                }
-                for (; b < m; b += 32) s0 = fmaf(__ldg(Srow + b), v[b], s0);
-            }
-            float s = s0 + s1;
-#pragma unroll
-            for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
-            if (lane == 0) {
-                if (lc != acc_lc) {
-                    if (acc_lc >= 0)
-                        for (int q = 0; q < PST; ++q) wacc[wid][acc_lc][q] += acc[q];
-                    acc_lc = lc;
-                    for (int q = 0; q < PST; ++q) acc[q] = 0.0;
-                }
-                const double ra = p.r[(size_t)c * m + a];
-                const float yf = (float)((double)s + sh_corr[lc][0] * ra + sh_corr[lc][1]);
-                p.u[((size_t)un * k + c) * m + a] = yf;
-                acc[0] += (double)yf * yf;
-                acc[1] += (double)yf;
-                acc[2] += ra * (double)yf;
-                if (t >= 1) {
-                    const double d = (double)v[a] - (double)(__ldcg(p.u + ((size_t)up * k + c) * m + a) *
-                                                             (float)sh_corr[lc][2]);
-                    acc[3] += d * d;
-                }
-            }
-        }
-        if (lane == 0 && acc_lc >= 0)
-            for (int q = 0; q < PST; ++q) wacc[wid][acc_lc][q] += acc[q];
-        __syncthreads();
-        if (threadIdx.x < ncl * PST) {
-            const int lc = threadIdx.x / PST, q = threadIdx.x % PST;
-            const int c = c_lo + lc;
-            double sum = 0.0;
-            for (int w = 0; w < nw; ++w) sum += wacc[w][lc][q];
-            if (p.counts[c] != 0) atomicAdd(pst(p.st, k, t + 1, c) + q, sum);
-        }
-        grid_barrier(p.bar, G, gen, p.status);
-        // every block reads the same published step differences (in parallel)
-        double mx = 0;
-        if (t >= 1)
-            for (int c = threadIdx.x; c < k; c += blockDim.x)
-                if (p.counts[c] != 0) mx = fmax(mx, __ldcg(pst(p.st, k, t + 1, c) + 3));
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
-        if (lane == 0) wacc[wid][0][0] = mx;
-        __syncthreads();
-        if (threadIdx.x == 0) {
-            double all = 0;
-            for (int w = 0; w < nw; ++w) all = fmax(all, wacc[w][0][0]);
-            sh_done = t >= p.tmax || __ldcg(p.status) != 0 || (t >= 1 && all < p.tol2);
-        }
-        __syncthreads();
-        if (sh_done) {
-            if (blockIdx.x == 0 && threadIdx.x == 0) p.status[1] = t;
-            break;
-        }
-    }
-}
-
-// v = u_T/|u_T|, lambda = v . u_{T+1} (FP64).  lambda > 0: sign rule against the
-// cluster's first member a (flip when |a - v| >= |a + v|) and store (canonical:
-// re-z-normalised, ddof=1).  lambda <= 0 (M numerically zero): the last basis
-// vector - the last column of a symmetric eigensolver's identity basis - with the
-// same sign rule.  NaN: the centroid is left unchanged (neither branch of
-// shapeExtract.cuh:638-649 fires).
-__global__ void k_power_final(const float* __restrict__ u, const double* __restrict__ st,
-                              const int32_t* __restrict__ counts, const int32_t* __restrict__ offsets,
-                              const float* __restrict__ seg, int k, int m, int T, int mode,
-                              float* __restrict__ C, float* __restrict__ lambda_out) {
-    __shared__ double red[32];
-    __shared__ double sh_lam, sh_flip, sh_mean, sh_inv;
-    const int c = blockIdx.x;
-    if (counts[c] == 0) return;
-    const int sT = T % 3, sN = (T + 1) % 3;
-    const float* uT = u + ((size_t)sT * k + c) * m;
-    const float* uN = u + ((size_t)sN * k + c) * m;
-    const double nT = st[((size_t)(T & 3) * k + c) * PST];
-    const double invT = 1.0 / sqrt(nT);
-    const float* a = seg + (size_t)offsets[c] * m;
-    double lam = 0;
-    for (int i = threadIdx.x; i < m; i += blockDim.x) lam += (double)((float)(uT[i] * invT)) * (double)uN[i];
-    lam = block_sum_d(lam, red);
-    if (threadIdx.x == 0) sh_lam = lam;
-    __syncthreads();
-    lam = sh_lam;
-    if (!(lam > 0) && !(lam <= 0)) return;  // NaN
-    const bool degenerate = !(lam > 0);
-    double d1 = 0, d2 = 0, sum = 0;
-    for (int i = threadIdx.x; i < m; i += blockDim.x) {
-        double v = degenerate ? (i == m - 1 ? 1.0 : 0.0) : (double)((float)(uT[i] * invT));
-        double ai = a[i];
-        d1 += (ai - v) * (ai - v);
-        d2 += (ai + v) * (ai + v);
-        sum += v;
-    }
-    d1 = block_sum_d(d1, red);
-    d2 = block_sum_d(d2, red);
-    sum = block_sum_d(sum, red);
-    const double sgn = (sqrt(d1) >= sqrt(d2)) ? -1.0 : 1.0;
-    double mean = 0, inv = 1;
-    if (mode == TC_MODE_CANONICAL) {
-        mean = sgn * sum / m;
-        double ss = 0;
-        for (int i = threadIdx.x; i < m; i += blockDim.x) {
-            double v = sgn * (degenerate ? (i == m - 1 ? 1.0 : 0.0) : (double)((float)(uT[i] * invT)));
-            ss += (v - mean) * (v - mean);
-        }
-        ss = block_sum_d(ss, red);
-        double sd = sqrt(ss / (m - 1));
-        inv = sd > 0 ? 1.0 / sd : 0.0;
-    }
-    float* out = C + (size_t)c * m;
-    for (int i = threadIdx.x; i < m; i += blockDim.x) {
-        double v = sgn * (degenerate ? (i == m - 1 ? 1.0 : 0.0) : (double)((float)(uT[i] * invT)));
-        out[i] = (float)((v - mean) * inv);
-    }
-    if (threadIdx.x == 0 && lambda_out) lambda_out[c] = (float)lam;
-}
-
-// ---------------------------------------------------------------- power-iteration launch
-// Returns the step T whose vector is the eigenvector estimate (synchronises).
-static int run_power(tc_ctx* ctx, const float* S, const double* r, const double* tot, const int32_t* counts, int k,
-                     int m, int tmax, double tol, float* u, double* st, cudaStream_t s) {
-    int per_sm = 0;
-    int G = 0;
-    const int64_t R = (int64_t)k * m;
-    // blocks touch at most ncl clusters; their v vectors live in shared memory
-    auto ncl_max = [&](int g) {
-        int mx = 0;
-        for (int b = 0; b < g; ++b) {
-            int64_t r0 = R * b / g, r1 = R * (b + 1) / g;
-            if (r1 > r0) mx = std::max(mx, (int)((r1 - 1) / m - r0 / m + 1));
-        }
-        return mx;
-    };
-    size_t smem = 0;
-    for (int pass = 0; pass < 2; ++pass) {
-        G = pass == 0 ? ctx->sm_count : ctx->sm_count * std::max(per_sm, 1);
-        smem = (size_t)ncl_max(G) * m * sizeof(float);
-        TC_REQUIRE(ncl_max(G) <= 8 && smem + 1024 <= ctx->smem_optin, TC_ERR_UNSUPPORTED,
-                   "power iteration: k*m too large for the persistent kernel");
-        TC_CUDA(cudaFuncSetAttribute(k_power_persistent, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-        TC_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_power_persistent, 1024, smem));
-        TC_REQUIRE(per_sm >= 1, TC_ERR_UNSUPPORTED, "power iteration kernel does not fit on an SM");
-        if (per_sm == 1) break;
-    }
-    int32_t* status = reinterpret_cast<int32_t*>(ctx->ws.aux.as<char>(64) + 32);
-    unsigned* bar = reinterpret_cast<unsigned*>(status + 2);
-    TC_CUDA(cudaMemsetAsync(status, 0, 16, s));
-    PowerParams pp{S, r, tot, counts, k, m, tmax, tol * tol, u, st, bar, status};
-    void* args[] = {&pp};
-    TC_CUDA(cudaLaunchCooperativeKernel((const void*)k_power_persistent, dim3(G), dim3(1024), args, smem, s));
-    TC_CHECK_LAUNCH();
-    int32_t h[2];
-    TC_CUDA(cudaMemcpyAsync(h, status, sizeof(h), cudaMemcpyDeviceToHost, s));
-    TC_CUDA(cudaStreamSynchronize(s));
-    TC_REQUIRE(h[0] == 0, TC_ERR_TIMEOUT, "power iteration: grid barrier wait ran out");
-    return h[1];
-}
+void power_eigvecs(tc_ctx* ctx, const float* S, const double* r, const double* tot, const int32_t* counts,
+                   const int32_t* offsets, const float* seg, int k, int m, int mode, int tmax, double tol, float* C,
+                   cudaStream_t s);
 
 // ---------------------------------------------------------------- driver
 int run_extract(tc_ctx* ctx, const ExtractArgs& a, cudaStream_t s) {
@@ -582,8 +282,6 @@ int run_extract(tc_ctx* ctx, const ExtractArgs& a, cudaStream_t s) {
     float* S = ws.gram.as<float>((size_t)k * m * m);
     double* rs = ws.rowsum.as<double>((size_t)k * m + k);
     double* tot = rs + (size_t)k * m;
-    float* u = ws.piter.as<float>((size_t)3 * k * m);
-    double* st = ws.pstats.as<double>((size_t)4 * PST * k);
 
     TC_CUDA(cudaMemsetAsync(scal, 0, sizeof(int32_t) * 16, s));
     if (n > 0) {
@@ -659,11 +357,7 @@ int run_extract(tc_ctx* ctx, const ExtractArgs& a, cudaStream_t s) {
     const bool full = a.cal_select || a.mode == TC_MODE_CANONICAL;
     const int tmax = full ? std::max(4 * m, 200) : m;
     const double tol = full ? 5e-7 : 1e-6;
-    k_power_prep<<<k, 256, 0, s>>>(counts, rs, k, m, u, st);
-    TC_CHECK_LAUNCH();
-    const int T = run_power(ctx, S, rs, tot, counts, k, m, tmax, tol, u, st, s);
-    k_power_final<<<k, 256, 0, s>>>(u, st, counts, offsets, seg, k, m, T, a.mode, a.C, nullptr);
-    TC_CHECK_LAUNCH();
+    power_eigvecs(ctx, S, rs, tot, counts, offsets, seg, k, m, a.mode, tmax, tol, a.C, s);
     return h_sc[0];
 }
 
