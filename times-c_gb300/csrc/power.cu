@@ -16,6 +16,8 @@
 // than tol, or at t = tmax.
 #include <algorithm>
 #include <cmath>
+#include <cstdio>
+#include <cstdlib>
 
 #include "tc_internal.h"
 
@@ -104,14 +106,17 @@ __device__ __forceinline__ void grid_barrier(unsigned* bar, unsigned nblocks, un
 
 // Dynamic shared memory of the persistent kernel, 16-byte aligned sections:
 // [S rows (RES only)] [v of the block's clusters] [v_{t-1} at own rows] [per-warp sums]
+// [r at own rows] [cluster sizes]
 struct PowerLayout {
-    size_t sv, vprev, wacc, total;
-    __host__ __device__ PowerLayout(bool res, int rows_max, int ncl_max, int m) {
+    size_t sv, vprev, wacc, rown, cnt, total;
+    __host__ __device__ PowerLayout(bool res, int rows_max, int ncl_max, int m, int k) {
         auto a16 = [](size_t x) { return (x + 15) & ~size_t(15); };
         sv = res ? a16((size_t)rows_max * m * 4) : 0;
         vprev = sv + a16((size_t)ncl_max * m * 4);
         wacc = vprev + a16((size_t)rows_max * 4);
-        total = wacc + (size_t)32 * ncl_max * PST * 8;
+        rown = wacc + a16((size_t)32 * ncl_max * PST * 8);
+        cnt = rown + a16((size_t)rows_max * 8);
+        total = cnt + a16((size_t)k * 4);
     }
 };
 
@@ -119,14 +124,18 @@ template <bool RES>
 __global__ void __launch_bounds__(1024, 1) k_power_persistent(PowerParams p) {
     extern __shared__ __align__(16) unsigned char dsm[];
     const int k = p.k, m = p.m;
-    const PowerLayout L(RES, p.rows_max, p.ncl_max, m);
+    const PowerLayout L(RES, p.rows_max, p.ncl_max, m, k);
     float* S_res = reinterpret_cast<float*>(dsm);
     float* sv = reinterpret_cast<float*>(dsm + L.sv);        // v of the block's clusters
     float* vprev = reinterpret_cast<float*>(dsm + L.vprev);  // v_{t-1} at the block's own rows
     double* wacc = reinterpret_cast<double*>(dsm + L.wacc);  // [warp][lc][PST]
+    double* r_own = reinterpret_cast<double*>(dsm + L.rown); // r at the block's own rows
+    int* cnt = reinterpret_cast<int*>(dsm + L.cnt);          // cluster sizes
+    __shared__ double sh_stat[8][4];  // per local cluster: |u|^2, sum u, r.u of the loaded step; tot
     __shared__ double sh_corr[8][2];
+    __shared__ float sh_inv[8];
     __shared__ double red[32];
-    __shared__ int sh_done;
+    __shared__ int sh_done, sh_status;
     const int64_t R = (int64_t)k * m;
     const unsigned G = gridDim.x;
     const int64_t r0 = R * blockIdx.x / G, r1 = R * (blockIdx.x + 1) / G;
@@ -135,29 +144,55 @@ __global__ void __launch_bounds__(1024, 1) k_power_persistent(PowerParams p) {
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
     unsigned gen = 0;
 
-    if (RES) {  // the block's rows of S stay in shared memory for every step
+    // constants of the whole iteration live in shared memory (L1 is tiny next to them)
+    for (int e = threadIdx.x; e < k; e += blockDim.x) cnt[e] = p.counts[e];
+    for (int64_t e = threadIdx.x; e < r1 - r0; e += blockDim.x) r_own[e] = p.r[r0 + e];  // r is [c][a] = row order
+    if (threadIdx.x < ncl) sh_stat[threadIdx.x][3] = p.tot[c_lo + threadIdx.x];
+    if (RES) {
         const int64_t nval = (r1 - r0) * m;
         const float* src = p.S + (size_t)r0 * m;
         for (int64_t e = threadIdx.x; e < nval; e += blockDim.x) S_res[e] = __ldg(src + e);
     }
-    // v_t of the block's clusters and its centring terms, from u slot t%3 / stats slot t
-    auto load_v = [&](int t) {
-        for (int lc = 0; lc < ncl; ++lc) {
-            const int c = c_lo + lc;
-            if (p.counts[c] == 0) continue;
-            const double* sc = pst(p.st, k, t, c);
-            const double inv = 1.0 / sqrt(__ldcg(sc));
-            const float finv = (float)inv;
-            const float* ut = p.u + ((size_t)(t % 3) * k + c) * m;
-            for (int b = threadIdx.x; b < m; b += blockDim.x) sv[(size_t)lc * m + b] = __ldcg(ut + b) * finv;
-            if (threadIdx.x == 0) {
-                const double s1 = __ldcg(sc + 1) * inv, s2 = __ldcg(sc + 2) * inv, mm = (double)m;
-                sh_corr[lc][0] = -s1 / mm;
-                sh_corr[lc][1] = -s2 / mm + p.tot[c] * s1 / (mm * mm);
-            }
+    __syncthreads();
+
+    // Loads v_t (from u slot t%3 and stats slot t&3) for the block's clusters and,
+    // in the same round trip, every cluster's step difference stored in that slot.
+    // Returns the largest difference (0 when want_delta is false).
+    auto load_step = [&](int t, bool want_delta) -> double {
+        const int ncm = ncl * m;
+        for (int e = threadIdx.x; e < ncm; e += blockDim.x) {
+            const int lc = e / m, c = c_lo + lc;
+            sv[e] = cnt[c] ? __ldcg(p.u + ((size_t)(t % 3) * k + c) * m + (e - lc * m)) : 0.f;
         }
+        if (threadIdx.x < ncl * 3) {
+            const int lc = threadIdx.x / 3, q = threadIdx.x % 3;
+            sh_stat[lc][q] = __ldcg(pst(p.st, k, t, c_lo + lc) + q);
+        }
+        if (threadIdx.x == 0) sh_status = __ldcg(p.status);
+        double mx = 0;
+        if (want_delta)
+            for (int c = threadIdx.x; c < k; c += blockDim.x)
+                if (cnt[c] != 0) mx = fmax(mx, __ldcg(pst(p.st, k, t, c) + 3));
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+        if (lane == 0) red[wid] = mx;
+        __syncthreads();
+        if (threadIdx.x < ncl) {
+            const int lc = threadIdx.x;
+            const double inv = 1.0 / sqrt(sh_stat[lc][0]);
+            const double s1 = sh_stat[lc][1] * inv, s2 = sh_stat[lc][2] * inv, mm = (double)m;
+            sh_inv[lc] = (float)inv;
+            sh_corr[lc][0] = -s1 / mm;
+            sh_corr[lc][1] = -s2 / mm + sh_stat[lc][3] * s1 / (mm * mm);
+        }
+        double all = 0;
+        for (int w = 0; w < nw; ++w) all = fmax(all, red[w]);
+        __syncthreads();
+        for (int e = threadIdx.x; e < ncm; e += blockDim.x) sv[e] *= sh_inv[e / m];
+        __syncthreads();
+        return all;
     };
-    load_v(0);
+    load_step(0, false);
     for (int t = 0;; ++t) {
         const int un = (t + 1) % 3;
         for (int e = threadIdx.x; e < nw * p.ncl_max * PST; e += blockDim.x) wacc[e] = 0.0;
@@ -166,37 +201,33 @@ __global__ void __launch_bounds__(1024, 1) k_power_persistent(PowerParams p) {
         int acc_lc = -1;
         for (int64_t row = r0 + wid; row < r1; row += nw) {
             const int c = (int)(row / m), a = (int)(row % m), lc = c - c_lo;
-            if (p.counts[c] == 0) continue;
+            if (cnt[c] == 0) continue;
             const float* Srow = RES ? S_res + (size_t)(row - r0) * m : p.S + (size_t)row * m;
             const float* v = sv + (size_t)lc * m;
-            float s0 = 0.f, s1 = 0.f;
+            // compensated (Kahan) lane sums, FP64 across lanes: rounding noise well
+            // below the convergence tolerance
+            float s = 0.f, comp = 0.f;
+            auto add = [&](float x) {
+                const float y = x - comp, tt = s + y;
+                comp = (tt - s) - y;
+                s = tt;
+            };
             if ((m & 3) == 0) {
                 const float4* S4 = reinterpret_cast<const float4*>(Srow);
                 const float4* v4 = reinterpret_cast<const float4*>(v);
-                int b = lane;
-                for (; b + 32 < m / 4; b += 64) {
-                    float4 x0, x1;
-                    if (RES) { x0 = S4[b]; x1 = S4[b + 32]; }
-                    else { x0 = __ldg(S4 + b); x1 = __ldg(S4 + b + 32); }
-                    const float4 w0 = v4[b], w1 = v4[b + 32];
-                    s0 = fmaf(x0.x, w0.x, s0); s0 = fmaf(x0.y, w0.y, s0); s0 = fmaf(x0.z, w0.z, s0); s0 = fmaf(x0.w, w0.w, s0);
-                    s1 = fmaf(x1.x, w1.x, s1); s1 = fmaf(x1.y, w1.y, s1); s1 = fmaf(x1.z, w1.z, s1); s1 = fmaf(x1.w, w1.w, s1);
-                }
-                for (; b < m / 4; b += 32) {
-                    const float4 x0 = RES ? S4[b] : __ldg(S4 + b), w0 = v4[b];
-                    s0 = fmaf(x0.x, w0.x, s0); s0 = fmaf(x0.y, w0.y, s0); s0 = fmaf(x0.z, w0.z, s0); s0 = fmaf(x0.w, w0.w, s0);
+                for (int b = lane; b < m / 4; b += 32) {
+                    const float4 x = RES ? S4[b] : __ldg(S4 + b), w = v4[b];
+                    add(x.x * w.x);
+                    add(x.y * w.y);
+                    add(x.z * w.z);
+                    add(x.w * w.w);
                 }
             } else {
-                int b = lane;
-                for (; b + 32 < m; b += 64) {
-                    s0 = fmaf(RES ? Srow[b] : __ldg(Srow + b), v[b], s0);
-                    s1 = fmaf(RES ? Srow[b + 32] : __ldg(Srow + b + 32), v[b + 32], s1);
-                }
-                for (; b < m; b += 32) s0 = fmaf(RES ? Srow[b] : __ldg(Srow + b), v[b], s0);
+                for (int b = lane; b < m; b += 32) add((RES ? Srow[b] : __ldg(Srow + b)) * v[b]);
             }
-            float s = s0 + s1;
+            double ds = (double)s - (double)comp;
 #pragma unroll
-            for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+            for (int o = 16; o > 0; o >>= 1) ds += __shfl_xor_sync(0xffffffffu, ds, o);
             if (lane == 0) {
                 if (lc != acc_lc) {
                     if (acc_lc >= 0)
@@ -204,8 +235,8 @@ __global__ void __launch_bounds__(1024, 1) k_power_persistent(PowerParams p) {
                     acc_lc = lc;
                     for (int q = 0; q < PST; ++q) acc[q] = 0.0;
                 }
-                const double ra = p.r[(size_t)c * m + a];
-                const float yf = (float)((double)s + sh_corr[lc][0] * ra + sh_corr[lc][1]);
+                const double ra = r_own[row - r0];
+                const float yf = (float)(ds + sh_corr[lc][0] * ra + sh_corr[lc][1]);
                 p.u[((size_t)un * k + c) * m + a] = yf;
                 acc[0] += (double)yf * yf;
                 acc[1] += (double)yf;
@@ -226,24 +257,11 @@ __global__ void __launch_bounds__(1024, 1) k_power_persistent(PowerParams p) {
             const int c = c_lo + lc;
             double sum = 0.0;
             for (int w = 0; w < nw; ++w) sum += wacc[((size_t)w * p.ncl_max + lc) * PST + q];
-            if (p.counts[c] != 0) atomicAdd(pst(p.st, k, t + 1, c) + q, sum);
+            if (cnt[c] != 0) atomicAdd(pst(p.st, k, t + 1, c) + q, sum);
         }
         grid_barrier(p.bar, G, gen, p.status);
-        // next vector and every cluster's step difference, loaded together
-        load_v(t + 1);
-        double mx = 0;
-        if (t >= 1)
-            for (int c = threadIdx.x; c < k; c += blockDim.x)
-                if (p.counts[c] != 0) mx = fmax(mx, __ldcg(pst(p.st, k, t + 1, c) + 3));
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
-        if (lane == 0) red[wid] = mx;
-        __syncthreads();
-        if (threadIdx.x == 0) {
-            double all = 0;
-            for (int w = 0; w < nw; ++w) all = fmax(all, red[w]);
-            sh_done = t >= p.tmax || __ldcg(p.status) != 0 || (t >= 1 && all < p.tol2);
-        }
+        const double dmax = load_step(t + 1, t >= 1);
+        if (threadIdx.x == 0) sh_done = t >= p.tmax || sh_status != 0 || (t >= 1 && dmax < p.tol2);
         __syncthreads();
         if (sh_done) {
             if (blockIdx.x == 0 && threadIdx.x == 0) p.status[1] = t;
@@ -336,9 +354,9 @@ void power_eigvecs(tc_ctx* ctx, const float* S, const double* r, const double* t
         if (r1 > r0) ncl_max = std::max(ncl_max, (int)((r1 - 1) / m - r0 / m + 1));
     }
     TC_REQUIRE(ncl_max <= 8, TC_ERR_UNSUPPORTED, "power iteration: more than 8 clusters per block");
-    const size_t res_bytes = PowerLayout(true, rows_max, ncl_max, m).total;
+    const size_t res_bytes = PowerLayout(true, rows_max, ncl_max, m, k).total;
     const bool res = res_bytes + 2048 <= ctx->smem_optin;
-    const size_t smem = PowerLayout(res, rows_max, ncl_max, m).total;
+    const size_t smem = PowerLayout(res, rows_max, ncl_max, m, k).total;
     TC_REQUIRE(smem + 2048 <= ctx->smem_optin, TC_ERR_UNSUPPORTED, "power iteration: k*m too large");
     int per_sm = 0;
     if (res) {
@@ -359,6 +377,9 @@ void power_eigvecs(tc_ctx* ctx, const float* S, const double* r, const double* t
     TC_CUDA(cudaMemcpyAsync(h, status, sizeof(h), cudaMemcpyDeviceToHost, s));
     TC_CUDA(cudaStreamSynchronize(s));
     TC_REQUIRE(h[0] == 0, TC_ERR_TIMEOUT, "power iteration: grid barrier wait ran out");
+    if (std::getenv("TIMESC_TRACE"))
+        std::fprintf(stderr, "timesc: power iteration k=%d m=%d steps=%d of %d (%s)\n", k, m, h[1], tmax,
+                     res ? "S in shared memory" : "S streamed");
     k_power_final<<<k, 256, 0, s>>>(u, st, counts, offsets, seg, k, m, h[1], mode, C);
     TC_CHECK_LAUNCH();
 }
