@@ -26,8 +26,8 @@ void launch_gather_norm(const float* x, const int32_t* perm, const int32_t* labe
                         const uint8_t* gate, int64_t n, int m, float* seg, int sm_count, cudaStream_t s);
 bool gram_tc_supported(int m, int precision);
 void launch_gram_tc(tc_ctx* ctx, const float* seg, const int32_t* counts, const int32_t* offsets,
-                    const std::vector<int32_t>& h_counts, int64_t n, int k, int m, int precision, float* S,
-                    cudaStream_t s);
+                    const std::vector<int32_t>& h_counts, int64_t n, int k, int m, int ld, int precision,
+                    float* S, cudaStream_t s);
 
 constexpr int SEG_CHUNK = 4096;
 constexpr int SEG_BLOCK = 256;
@@ -172,7 +172,7 @@ __global__ void k_gate(const float* __restrict__ C, int m, int mode, uint8_t* __
 // 64x64 output tiles of the upper triangle, 256 threads x 4x4 outputs, K in
 // 32-row slabs; FP32 sums of 256 rows are folded into a compensated total.
 __global__ void __launch_bounds__(256) k_gram_simt(const float* __restrict__ Y, const int32_t* __restrict__ counts,
-                                                   const int32_t* __restrict__ offsets, int m, int nt,
+                                                   const int32_t* __restrict__ offsets, int m, int ld, int nt,
                                                    float* __restrict__ S) {
     __shared__ __align__(16) float As[32][64];
     __shared__ __align__(16) float Bs[32][64];
@@ -226,29 +226,29 @@ __global__ void __launch_bounds__(256) k_gram_simt(const float* __restrict__ Y, 
                 }
         }
     }
-    float* Sc = S + (size_t)c * m * m;
+    float* Sc = S + (size_t)c * m * ld;
 #pragma unroll
     for (int i = 0; i < 4; ++i)
 #pragma unroll
         for (int j = 0; j < 4; ++j) {
             int a = a0 + ty * 4 + i, b = b0 + tx * 4 + j;
             if (a < m && b < m) {
-                Sc[(size_t)a * m + b] = tot[i][j];
-                Sc[(size_t)b * m + a] = tot[i][j];
+                Sc[(size_t)a * ld + b] = tot[i][j];
+                Sc[(size_t)b * ld + a] = tot[i][j];
             }
         }
 }
 
 // ---------------------------------------------------------------- centring terms
 // r[c][a] = sum_b S[c][a][b] (FP64), tot[c] = sum_a r[c][a]
-__global__ void k_rowsum(const float* __restrict__ S, const int32_t* __restrict__ counts, int m,
+__global__ void k_rowsum(const float* __restrict__ S, const int32_t* __restrict__ counts, int m, int ld,
                          double* __restrict__ r, double* __restrict__ tot) {
     const int c = blockIdx.y;
     if (counts[c] == 0) return;
     const int lane = threadIdx.x & 31;
     const int a = blockIdx.x * 8 + (threadIdx.x >> 5);
     if (a >= m) return;
-    const float* row = S + ((size_t)c * m + a) * m;
+    const float* row = S + ((size_t)c * m + a) * ld;
     float s = 0.f;
     for (int b = lane; b < m; b += 32) s += row[b];
     double d = s;
@@ -260,7 +260,7 @@ __global__ void k_rowsum(const float* __restrict__ S, const int32_t* __restrict_
     }
 }
 
-void power_eigvecs(tc_ctx* ctx, const float* S, const double* r, const double* tot, const int32_t* counts,
+void power_eigvecs(tc_ctx* ctx, const float* S, int ld, const double* r, const double* tot, const int32_t* counts,
                    const int32_t* offsets, const float* seg, int k, int m, int mode, int tmax, double tol, float* C,
                    cudaStream_t s);
 
@@ -279,7 +279,8 @@ int run_extract(tc_ctx* ctx, const ExtractArgs& a, cudaStream_t s) {
     uint8_t* gate = ws.gate.as<uint8_t>(k);
     int32_t* scal = ws.scal.as<int32_t>(16);
     float* seg = ws.seg.as<float>((size_t)std::max<int64_t>(n, 1) * m);
-    float* S = ws.gram.as<float>((size_t)k * m * m);
+    const int ld = (m + 3) & ~3;  // Gram row pitch: rows stream as float4
+    float* S = ws.gram.as<float>((size_t)k * m * ld);
     double* rs = ws.rowsum.as<double>((size_t)k * m + k);
     double* tot = rs + (size_t)k * m;
 
@@ -338,17 +339,18 @@ int run_extract(tc_ctx* ctx, const ExtractArgs& a, cudaStream_t s) {
     launch_gather_norm(a.x, perm, a.labels, any_gate ? shift : nullptr, any_gate ? gate : nullptr, n, m, seg,
                        ctx->sm_count, s);
 
-    // Gram
+    // Gram (padding columns b in [m, ld) stay zero)
+    if (ld != m) TC_CUDA(cudaMemsetAsync(S, 0, sizeof(float) * (size_t)k * m * ld, s));
     const int nt = ceil_div(m, 64);
     if (gram_tc_supported(m, a.precision)) {
-        launch_gram_tc(ctx, seg, counts, offsets, h_counts, n, k, m, a.precision, S, s);
+        launch_gram_tc(ctx, seg, counts, offsets, h_counts, n, k, m, ld, a.precision, S, s);
     } else {
         dim3 g(nt * (nt + 1) / 2, k);
-        k_gram_simt<<<g, 256, 0, s>>>(seg, counts, offsets, m, nt, S);
+        k_gram_simt<<<g, 256, 0, s>>>(seg, counts, offsets, m, ld, nt, S);
         TC_CHECK_LAUNCH();
     }
     TC_CUDA(cudaMemsetAsync(tot, 0, sizeof(double) * k, s));
-    k_rowsum<<<dim3(ceil_div(m, 8), k), 256, 0, s>>>(S, counts, m, rs, tot);
+    k_rowsum<<<dim3(ceil_div(m, 8), k), 256, 0, s>>>(S, counts, m, ld, rs, tot);
     TC_CHECK_LAUNCH();
 
     // power iteration: compat runs at most m steps (the reference's fixed count),
@@ -357,7 +359,7 @@ int run_extract(tc_ctx* ctx, const ExtractArgs& a, cudaStream_t s) {
     const bool full = a.cal_select || a.mode == TC_MODE_CANONICAL;
     const int tmax = full ? std::max(4 * m, 200) : m;
     const double tol = full ? 5e-7 : 1e-6;
-    power_eigvecs(ctx, S, rs, tot, counts, offsets, seg, k, m, a.mode, tmax, tol, a.C, s);
+    power_eigvecs(ctx, S, ld, rs, tot, counts, offsets, seg, k, m, a.mode, tmax, tol, a.C, s);
     return h_sc[0];
 }
 

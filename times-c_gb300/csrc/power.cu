@@ -3,9 +3,20 @@
 // of get_center, :217-264).
 //
 // M v = S v - (1.v/m) r - (r.v/m) 1 + (tot 1.v/m^2) 1 with r = S 1 and tot = 1^T S 1,
-// so M is never formed.  Step t: v_t = u_t/|u_t|, u_{t+1} = M v_t: compensated FP32
-// dot products summed across lanes in FP64; norms, sums, the step difference and
-// the Rayleigh quotient in FP64.
+// so M is never formed.  Step t: v_t = u_t/|u_t|, u_{t+1} = M v_t.
+//
+// One thread-block cluster of CL CTAs per k-Shape cluster c.  CTA `rank` owns rows
+// [rank*m/CL, (rank+1)*m/CL) of S_c and streams them (float4, row pitch ld) from
+// L2/HBM every step.  Each CTA keeps the whole current vector in shared memory;
+// the new entries and the per-CTA partial sums are stored straight into every
+// CTA's shared memory (distributed shared memory), and one hardware cluster
+// barrier per step makes them visible.  Every CTA sums the partials in rank order,
+// so all CTAs hold bit-identical norms and take the same stop decision; clusters
+// stop independently.  Rank 0 finishes: Rayleigh quotient, sign rule, store.
+//
+// Arithmetic: row dot products are compensated FP32 (Kahan per lane, TwoSum
+// across lanes); the norm, the sums and the step difference are accumulated in
+// FP64, so rounding noise in |v_t - v_{t-1}| stays well below the tolerance.
 #include <cooperative_groups.h>
 
 #include <algorithm>
@@ -18,20 +29,12 @@
 
 namespace tc {
 
-// ---------------------------------------------------------------- cluster kernel
-// One thread-block cluster of CL CTAs per k-Shape cluster c.  CTA `rank` owns rows
-// [rank*m/CL, (rank+1)*m/CL) of S_c and streams them from L2/HBM every step.  Each
-// CTA keeps the whole current vector v_t in shared memory; the new entries y_a and
-// the per-CTA partial sums are stored straight into every CTA's shared memory
-// (distributed shared memory), and one hardware cluster barrier per step makes
-// them visible.  Every CTA then sums the partials in rank order, so all CTAs hold
-// bit-identical norms and make the same stop decision.  Clusters stop
-// independently.  Rank 0 finishes: lambda, sign rule, store.
 constexpr int PC_THREADS = 512;
 constexpr int PC_UNROLL = 4;  // rows in flight per warp
 
 struct PowerClusterParams {
     const float* S;
+    int ld;
     const double* r;
     const double* tot;
     const int32_t* counts;
@@ -43,32 +46,51 @@ struct PowerClusterParams {
     int* steps;  // per cluster: the step T whose vector was stored (diagnostics)
 };
 
+// (s, c) += (s2, c2) where a pair means s - c; the two leading parts are added
+// error-free (TwoSum) and the rounding error folded into c.
+__device__ __forceinline__ void two_sum_acc(float& s, float& c, float s2, float c2) {
+    const float t = s + s2;
+    const float bp = t - s;
+    const float err = (s - (t - bp)) + (s2 - bp);
+    s = t;
+    c = c + c2 - err;
+}
+
+// 1/sqrt(x) to double precision: FP32 estimate and two Newton steps.
+__device__ __forceinline__ double rsqrt_d(double x) {
+    double y = (double)rsqrtf((float)x);
+    y = y * (1.5 - 0.5 * x * y * y);
+    y = y * (1.5 - 0.5 * x * y * y);
+    return y;
+}
+
 template <int CL>
 __global__ void __launch_bounds__(PC_THREADS) k_power_cluster(PowerClusterParams p) {
     namespace cg = cooperative_groups;
     cg::cluster_group cluster = cg::this_cluster();
     extern __shared__ __align__(16) unsigned char dsm[];
-    const int m = p.m;
+    const int m = p.m, ld = p.ld;
     const int rank = (int)cluster.block_rank();
     const int c = blockIdx.x / CL;
     if (p.counts[c] == 0) return;  // every CTA of this cluster leaves together
     const int a0 = (int)((int64_t)rank * m / CL), a1 = (int)((int64_t)(rank + 1) * m / CL);
     const int nrow = a1 - a0;
-    // shared memory: v[m] | y[2][m] | part[2][CL][4] doubles | vprev[nrow] | r_own[nrow] doubles
+    // shared memory: v[ld] | y[2][ld] | part[2][CL][4] doubles | vprev[nrow] | r_own[nrow]
     auto a16 = [](size_t x) { return (x + 15) & ~size_t(15); };
     float* v = reinterpret_cast<float*>(dsm);
-    float* ybuf = reinterpret_cast<float*>(dsm + a16((size_t)m * 4));
-    double* part = reinterpret_cast<double*>(dsm + a16((size_t)m * 4) + a16((size_t)2 * m * 4));
+    float* ybuf = reinterpret_cast<float*>(dsm + a16((size_t)ld * 4));
+    double* part = reinterpret_cast<double*>(dsm + a16((size_t)ld * 4) + a16((size_t)2 * ld * 4));
     float* vprev = reinterpret_cast<float*>(reinterpret_cast<unsigned char*>(part) + a16((size_t)2 * CL * 4 * 8));
-    double* r_own = reinterpret_cast<double*>(reinterpret_cast<unsigned char*>(vprev) + a16((size_t)nrow * 4));
+    float* r_own = vprev + a16((size_t)nrow * 4) / 4;
     __shared__ double red[PC_THREADS / 32][4];
-    __shared__ double sh_corr[2];
+    __shared__ float sh_corr[2];
+    __shared__ double sh_inv;
     __shared__ int sh_done;
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = PC_THREADS / 32;
     const double* rc = p.r + (size_t)c * m;
-    const float* Sc = p.S + (size_t)c * m * m;
-    const double mm = (double)m, totc = p.tot[c];
-    for (int i = threadIdx.x; i < nrow; i += PC_THREADS) r_own[i] = rc[a0 + i];
+    const float* Sc = p.S + (size_t)c * m * ld;
+    const double inv_m = 1.0 / (double)m, totc = p.tot[c];
+    for (int i = threadIdx.x; i < nrow; i += PC_THREADS) r_own[i] = (float)rc[a0 + i];
 
     // v_0 = [1, .5, 1, .5, ...] / |.|, with its sum and r.v (identical in every CTA)
     {
@@ -90,59 +112,52 @@ __global__ void __launch_bounds__(PC_THREADS) k_power_cluster(PowerClusterParams
         if (threadIdx.x == 0) {
             double t2 = 0, t1 = 0, tr = 0;
             for (int w = 0; w < nw; ++w) { t2 += red[w][0]; t1 += red[w][1]; tr += red[w][2]; }
-            const double inv = 1.0 / sqrt(t2);
-            sh_corr[0] = -(t1 * inv) / mm;
-            sh_corr[1] = -(tr * inv) / mm + totc * (t1 * inv) / (mm * mm);
-            red[0][3] = inv;
+            const double inv = rsqrt_d(t2), sv = t1 * inv, rv = tr * inv;
+            sh_corr[0] = (float)(-sv * inv_m);
+            sh_corr[1] = (float)(-rv * inv_m + totc * sv * inv_m * inv_m);
+            sh_inv = inv;
         }
         __syncthreads();
-        const float finv = (float)red[0][3];
-        for (int a = threadIdx.x; a < m; a += PC_THREADS) v[a] = ((a % 2 == 0) ? 1.0f : 0.5f) * finv;
+        const float finv = (float)sh_inv;
+        for (int a = threadIdx.x; a < ld; a += PC_THREADS) v[a] = a < m ? ((a % 2 == 0) ? 1.0f : 0.5f) * finv : 0.f;
+        for (int a = threadIdx.x; a < 2 * ld; a += PC_THREADS) ybuf[a] = 0.f;  // padding stays zero
         __syncthreads();
     }
     float* yrem[CL];
     double* prem[CL];
+#pragma unroll
     for (int q = 0; q < CL; ++q) {
         yrem[q] = cluster.map_shared_rank(ybuf, q);
         prem[q] = cluster.map_shared_rank(part, q);
     }
     cluster.sync();  // every CTA initialised before remote stores start
     int T = p.tmax;
+    const float4* v4 = reinterpret_cast<const float4*>(v);
+    const int nv4 = ld / 4;
     for (int t = 0;; ++t) {
         const int par = t & 1;
+        const float cr = sh_corr[0], cc = sh_corr[1];
         double acc[4] = {0.0, 0.0, 0.0, 0.0};
-        // own rows, PC_UNROLL rows per warp in flight
         for (int i0 = wid * PC_UNROLL; i0 < nrow; i0 += nw * PC_UNROLL) {
             float s[PC_UNROLL], cp[PC_UNROLL];
+            const float4* rowp[PC_UNROLL];
 #pragma unroll
-            for (int u = 0; u < PC_UNROLL; ++u) { s[u] = 0.f; cp[u] = 0.f; }
-            if ((m & 3) == 0) {
-                const float4* v4 = reinterpret_cast<const float4*>(v);
-                for (int b = lane; b < m / 4; b += 32) {
-                    const float4 w = v4[b];
-                    float4 x[PC_UNROLL];
+            for (int u = 0; u < PC_UNROLL; ++u) {
+                s[u] = 0.f;
+                cp[u] = 0.f;
+                rowp[u] = reinterpret_cast<const float4*>(Sc + (size_t)(a0 + min(i0 + u, nrow - 1)) * ld);
+            }
+            for (int b = lane; b < nv4; b += 32) {
+                const float4 w = v4[b];
+                float4 x[PC_UNROLL];
 #pragma unroll
-                    for (int u = 0; u < PC_UNROLL; ++u)
-                        x[u] = (i0 + u < nrow) ? __ldg(reinterpret_cast<const float4*>(Sc + (size_t)(a0 + i0 + u) * m) + b)
-                                               : make_float4(0.f, 0.f, 0.f, 0.f);
+                for (int u = 0; u < PC_UNROLL; ++u) x[u] = __ldg(rowp[u] + b);
 #pragma unroll
-                    for (int u = 0; u < PC_UNROLL; ++u) {
-                        const float pr[4] = {x[u].x * w.x, x[u].y * w.y, x[u].z * w.z, x[u].w * w.w};
+                for (int u = 0; u < PC_UNROLL; ++u) {
+                    const float pr[4] = {x[u].x * w.x, x[u].y * w.y, x[u].z * w.z, x[u].w * w.w};
 #pragma unroll
-                        for (int e = 0; e < 4; ++e) {  // Kahan
-                            const float yk = pr[e] - cp[u], tt = s[u] + yk;
-                            cp[u] = (tt - s[u]) - yk;
-                            s[u] = tt;
-                        }
-                    }
-                }
-            } else {
-                for (int b = lane; b < m; b += 32) {
-                    const float w = v[b];
-#pragma unroll
-                    for (int u = 0; u < PC_UNROLL; ++u) {
-                        const float x = (i0 + u < nrow) ? __ldg(Sc + (size_t)(a0 + i0 + u) * m + b) : 0.f;
-                        const float yk = x * w - cp[u], tt = s[u] + yk;
+                    for (int e = 0; e < 4; ++e) {  // Kahan
+                        const float yk = pr[e] - cp[u], tt = s[u] + yk;
                         cp[u] = (tt - s[u]) - yk;
                         s[u] = tt;
                     }
@@ -150,23 +165,26 @@ __global__ void __launch_bounds__(PC_THREADS) k_power_cluster(PowerClusterParams
             }
 #pragma unroll
             for (int u = 0; u < PC_UNROLL; ++u) {
-                double ds = (double)s[u] - (double)cp[u];
 #pragma unroll
-                for (int o = 16; o > 0; o >>= 1) ds += __shfl_xor_sync(0xffffffffu, ds, o);
+                for (int o = 16; o > 0; o >>= 1) {
+                    const float s2 = __shfl_xor_sync(0xffffffffu, s[u], o);
+                    const float c2 = __shfl_xor_sync(0xffffffffu, cp[u], o);
+                    two_sum_acc(s[u], cp[u], s2, c2);
+                }
                 const int i = i0 + u;
                 if (i < nrow) {
                     const int a = a0 + i;
-                    const double ra = r_own[i];
-                    const float yf = (float)(ds + sh_corr[0] * ra + sh_corr[1]);
-                    if (lane < CL) yrem[lane][par * m + a] = yf;  // into every CTA of the cluster
+                    const float ra = r_own[i];
+                    const float yf = (s[u] - cp[u]) + fmaf(cr, ra, cc);
+                    if (lane < CL) yrem[lane][par * ld + a] = yf;  // into every CTA of the cluster
                     if (lane == 0) {
-                        acc[0] += (double)yf * yf;
+                        acc[0] = fma((double)yf, (double)yf, acc[0]);
                         acc[1] += (double)yf;
-                        acc[2] += ra * (double)yf;
+                        acc[2] = fma((double)ra, (double)yf, acc[2]);
                         const float va = v[a];
                         if (t >= 1) {
-                            const double d = (double)va - (double)vprev[i];
-                            acc[3] += d * d;
+                            const float d = va - vprev[i];
+                            acc[3] = fma((double)d, (double)d, acc[3]);
                         }
                         vprev[i] = va;
                     }
@@ -179,56 +197,50 @@ __global__ void __launch_bounds__(PC_THREADS) k_power_cluster(PowerClusterParams
         if (threadIdx.x < 4) {
             double sum = 0;
             for (int w = 0; w < nw; ++w) sum += red[w][threadIdx.x];
+#pragma unroll
             for (int q = 0; q < CL; ++q) prem[q][(par * CL + rank) * 4 + threadIdx.x] = sum;
         }
         cluster.sync();  // y and partials of step t visible in every CTA
-        // identical reductions in every CTA (rank order)
-        if (threadIdx.x == 0) {
+        if (threadIdx.x == 0) {  // identical in every CTA (rank order)
             double n2 = 0, sy = 0, ry = 0, dd = 0;
             for (int q = 0; q < CL; ++q) {
                 const double* pq = part + (par * CL + q) * 4;
                 n2 += pq[0]; sy += pq[1]; ry += pq[2]; dd += pq[3];
             }
-            const double inv = 1.0 / sqrt(n2);
-            sh_corr[0] = -(sy * inv) / mm;
-            sh_corr[1] = -(ry * inv) / mm + totc * (sy * inv) / (mm * mm);
-            red[0][0] = inv;
-            sh_done = t >= p.tmax || (t >= 1 && dd < p.tol2);
+            const double inv = rsqrt_d(n2), sv = sy * inv, rv = ry * inv;
+            sh_corr[0] = (float)(-sv * inv_m);
+            sh_corr[1] = (float)(-rv * inv_m + totc * sv * inv_m * inv_m);
+            sh_inv = inv;
+            sh_done = t >= p.tmax || (t >= 1 && dd < p.tol2) || !(n2 > 0);
         }
         __syncthreads();
         if (sh_done) {
             T = t;
             break;
         }
-        const float finv = (float)red[0][0];
-        const float* y = ybuf + par * m;
+        const float finv = (float)sh_inv;
+        const float* y = ybuf + par * ld;
         for (int a = threadIdx.x; a < m; a += PC_THREADS) v[a] = y[a] * finv;
         __syncthreads();
     }
     // v = v_T (unit), y = u_{T+1} = M v_T in ybuf[T&1]
     if (rank == 0) {
-        const float* y = ybuf + (T & 1) * m;
+        const float* y = ybuf + (T & 1) * ld;
         const float* am = p.seg + (size_t)p.offsets[c] * m;
-        double lam = 0, d1 = 0, d2 = 0, sum = 0;
-        for (int a = threadIdx.x; a < m; a += PC_THREADS) {
-            lam += (double)v[a] * (double)y[a];
-        }
+        double lam = 0;
+        for (int a = threadIdx.x; a < m; a += PC_THREADS) lam += (double)v[a] * (double)y[a];
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) lam += __shfl_xor_sync(0xffffffffu, lam, o);
         if (lane == 0) red[wid][0] = lam;
         __syncthreads();
-        if (threadIdx.x == 0) {
-            double l = 0;
-            for (int w = 0; w < nw; ++w) l += red[w][0];
-            red[0][3] = l;
-        }
-        __syncthreads();
-        lam = red[0][3];
+        lam = 0;
+        for (int w = 0; w < nw; ++w) lam += red[w][0];
         __syncthreads();
         const bool nan = !(lam > 0) && !(lam <= 0);
         const bool degenerate = !(lam > 0);
         if (!nan) {  // NaN: neither branch of shapeExtract.cuh:638-649 fires, the centroid stays
             auto vec = [&](int a) -> double { return degenerate ? (a == m - 1 ? 1.0 : 0.0) : (double)v[a]; };
+            double d1 = 0, d2 = 0, sum = 0;
             for (int a = threadIdx.x; a < m; a += PC_THREADS) {
                 const double va = vec(a), ai = am[a];
                 d1 += (ai - va) * (ai - va);
@@ -243,18 +255,13 @@ __global__ void __launch_bounds__(PC_THREADS) k_power_cluster(PowerClusterParams
             }
             if (lane == 0) { red[wid][0] = d1; red[wid][1] = d2; red[wid][2] = sum; }
             __syncthreads();
-            if (threadIdx.x == 0) {
-                double a1s = 0, a2s = 0, ss = 0;
-                for (int w = 0; w < nw; ++w) { a1s += red[w][0]; a2s += red[w][1]; ss += red[w][2]; }
-                const double sgn = (sqrt(a1s) >= sqrt(a2s)) ? -1.0 : 1.0;  // get_center
-                sh_corr[0] = sgn;
-                sh_corr[1] = sgn * ss / mm;  // mean of the signed vector
-            }
+            double a1s = 0, a2s = 0, ss = 0;
+            for (int w = 0; w < nw; ++w) { a1s += red[w][0]; a2s += red[w][1]; ss += red[w][2]; }
             __syncthreads();
-            const double sgn = sh_corr[0];
+            const double sgn = (sqrt(a1s) >= sqrt(a2s)) ? -1.0 : 1.0;  // get_center
             double mean = 0, inv = 1;
             if (p.mode == TC_MODE_CANONICAL) {
-                mean = sh_corr[1];
+                mean = sgn * ss * inv_m;
                 double sq = 0;
                 for (int a = threadIdx.x; a < m; a += PC_THREADS) {
                     const double x = sgn * vec(a) - mean;
@@ -262,7 +269,6 @@ __global__ void __launch_bounds__(PC_THREADS) k_power_cluster(PowerClusterParams
                 }
 #pragma unroll
                 for (int o = 16; o > 0; o >>= 1) sq += __shfl_xor_sync(0xffffffffu, sq, o);
-                __syncthreads();
                 if (lane == 0) red[wid][0] = sq;
                 __syncthreads();
                 double tq = 0;
@@ -282,6 +288,7 @@ __global__ void __launch_bounds__(PC_THREADS) k_power_cluster(PowerClusterParams
 template <int CL>
 static void launch_cluster(const PowerClusterParams& pp, int k, size_t smem, cudaStream_t s) {
     TC_CUDA(cudaFuncSetAttribute(k_power_cluster<CL>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    if (CL > 8) TC_CUDA(cudaFuncSetAttribute(k_power_cluster<CL>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3((unsigned)k * CL);
     cfg.blockDim = dim3(PC_THREADS);
@@ -298,18 +305,27 @@ static void launch_cluster(const PowerClusterParams& pp, int k, size_t smem, cud
     TC_CHECK_LAUNCH();
 }
 
-void power_eigvecs(tc_ctx* ctx, const float* S, const double* r, const double* tot, const int32_t* counts,
-                   const int32_t* offsets, const float* seg, int k, int m, int mode, int tmax, double tol, float* C,
-                   cudaStream_t s) {
-    constexpr int CL = 8;  // CTAs per k-Shape cluster (portable cluster size)
-    int* steps = ctx->ws.pstats.as<int>((size_t)k);
+template <int CL>
+static size_t cluster_smem(int m, int ld) {
     auto a16 = [](size_t x) { return (x + 15) & ~size_t(15); };
     const int nrow = (m + CL - 1) / CL;
-    const size_t smem = a16((size_t)m * 4) + a16((size_t)2 * m * 4) + a16((size_t)2 * CL * 4 * 8) +
-                        a16((size_t)nrow * 4) + (size_t)nrow * 8;
-    TC_REQUIRE(smem + 4096 <= ctx->smem_optin, TC_ERR_UNSUPPORTED, "power iteration: series too long");
-    PowerClusterParams pp{S, r, tot, counts, offsets, seg, C, k, m, tmax, mode, tol * tol, steps};
-    launch_cluster<CL>(pp, k, smem, s);
+    return a16((size_t)ld * 4) + a16((size_t)2 * ld * 4) + a16((size_t)2 * CL * 4 * 8) + a16((size_t)nrow * 4) +
+           (size_t)nrow * 4;
+}
+
+void power_eigvecs(tc_ctx* ctx, const float* S, int ld, const double* r, const double* tot, const int32_t* counts,
+                   const int32_t* offsets, const float* seg, int k, int m, int mode, int tmax, double tol, float* C,
+                   cudaStream_t s) {
+    int* steps = ctx->ws.pstats.as<int>((size_t)k);
+    PowerClusterParams pp{S, ld, r, tot, counts, offsets, seg, C, k, m, tmax, mode, tol * tol, steps};
+    // long series stream tens of MB per step from HBM: spread each over 16 SMs
+    if (m > 1024) {
+        const size_t smem = cluster_smem<16>(m, ld);
+        TC_REQUIRE(smem + 4096 <= ctx->smem_optin, TC_ERR_UNSUPPORTED, "power iteration: series too long");
+        launch_cluster<16>(pp, k, smem, s);
+    } else {
+        launch_cluster<8>(pp, k, cluster_smem<8>(m, ld), s);
+    }
     if (std::getenv("TIMESC_TRACE")) {
         std::vector<int> h(k);
         TC_CUDA(cudaMemcpyAsync(h.data(), steps, sizeof(int) * k, cudaMemcpyDeviceToHost, s));

@@ -113,7 +113,7 @@ __global__ void k_seg_transpose(const float* __restrict__ seg, int64_t n, int m,
 template <int FMT>
 __global__ void __launch_bounds__(128, 1) k_gram_tc(const __grid_constant__ CUtensorMap tmap,
                                                     const int32_t* __restrict__ counts,
-                                                    const int64_t* __restrict__ poff, int m, int nt,
+                                                    const int64_t* __restrict__ poff, int m, int ld, int nt,
                                                     float* __restrict__ S, int* __restrict__ err) {
     extern __shared__ uint8_t smem_raw[];
     __shared__ __align__(8) uint64_t full[GT_STAGES], empty[GT_STAGES], done;
@@ -183,7 +183,7 @@ __global__ void __launch_bounds__(128, 1) k_gram_tc(const __grid_constant__ CUte
     sm100::tc_fence_after();
     if (fin) {
         const int a = ta * GT_TILE + warp * 32 + lane;
-        float* Sc = S + (size_t)c * m * m;
+        float* Sc = S + (size_t)c * m * ld;
         for (int cb = 0; cb < 4; ++cb) {
             float r[32];
             sm100::tmem_ld32(tmem + ((uint32_t)(warp * 32) << 16) + cb * 32, r);
@@ -192,12 +192,12 @@ __global__ void __launch_bounds__(128, 1) k_gram_tc(const __grid_constant__ CUte
             if (a < m) {
 #pragma unroll
                 for (int j = 0; j < 32; ++j)
-                    if (b0 + j < m) Sc[(size_t)a * m + b0 + j] = r[j];
+                    if (b0 + j < m) Sc[(size_t)a * ld + b0 + j] = r[j];
             }
             if (ta != tb) {
 #pragma unroll
                 for (int j = 0; j < 32; ++j)
-                    if (b0 + j < m && a < m) Sc[(size_t)(b0 + j) * m + a] = r[j];
+                    if (b0 + j < m && a < m) Sc[(size_t)(b0 + j) * ld + a] = r[j];
             }
         }
     } else if (threadIdx.x == 0) {
@@ -215,8 +215,8 @@ bool gram_tc_supported(int m, int precision) {
 }
 
 void launch_gram_tc(tc_ctx* ctx, const float* seg, const int32_t* counts, const int32_t* offsets,
-                    const std::vector<int32_t>& h_counts, int64_t n, int k, int m, int precision, float* S,
-                    cudaStream_t s) {
+                    const std::vector<int32_t>& h_counts, int64_t n, int k, int m, int ld, int precision,
+                    float* S, cudaStream_t s) {
     Workspace& ws = ctx->ws;
     std::vector<int64_t> hp(k);
     int64_t Pp = 0;
@@ -248,10 +248,10 @@ void launch_gram_tc(tc_ctx* ctx, const float* seg, const int32_t* counts, const 
     dim3 grid(nt * (nt + 1) / 2, k);
     if (tf32) {
         TC_CUDA(cudaFuncSetAttribute(k_gram_tc<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, GT_SMEM));
-        k_gram_tc<2><<<grid, 128, GT_SMEM, s>>>(map, counts, poff, m, nt, S, err);
+        k_gram_tc<2><<<grid, 128, GT_SMEM, s>>>(map, counts, poff, m, ld, nt, S, err);
     } else {
         TC_CUDA(cudaFuncSetAttribute(k_gram_tc<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, GT_SMEM));
-        k_gram_tc<1><<<grid, 128, GT_SMEM, s>>>(map, counts, poff, m, nt, S, err);
+        k_gram_tc<1><<<grid, 128, GT_SMEM, s>>>(map, counts, poff, m, ld, nt, S, err);
     }
     TC_CHECK_LAUNCH();
     int h_err = 0;
