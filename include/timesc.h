@@ -93,6 +93,24 @@ int tc_sbd_assign(tc_ctx* ctx, const float* d_x, const float* d_centroids, int64
                   const int32_t* d_old_labels, int32_t* d_changed, double* d_dist_sum,
                   tc_stream stream);
 
+/* Allocation-free SBD assignment.  No counterpart in the reference.
+ * For callers that must not allocate device memory on the call path: a serving
+ * loop that reserved all HBM for resident jobs up front, or a latency-critical
+ * host thread that cannot take cudaMalloc's implicit device synchronisation.
+ * Same kernels and results as tc_sbd_assign with precision TC_PREC_FP32 (labels
+ * 0-based, d_dist may be NULL), but no context: the scratch (twiddle tables and
+ * centroid spectra, 2*(F/2) + k*(F/2+1) complex values, F = tc_fft_size(m, mode))
+ * lives in one static device array of TC_NOALLOC_SCRATCH_BYTES that every GPU
+ * loading the library holds until the process exits.  Larger requests return
+ * TC_ERR_UNSUPPORTED with a message in err (may be NULL).  Calls no cudaMalloc or
+ * cudaFree.  The first call on a device looks up the array's device address
+ * (cudaGetSymbolAddress); make that first call before any stream capture.  All
+ * calls share the array: calls that overlap on the GPU (other streams, other host
+ * threads) race on it - serialise them. */
+#define TC_NOALLOC_SCRATCH_BYTES (4u << 20)
+int tc_sbd_assign_noalloc(const float* d_x, const float* d_centroids, int64_t n, int m, int k, int mode,
+                          int32_t* d_labels, float* d_dist, tc_stream stream, char* err, int err_len);
+
 /* Shape extraction: groups the rows by label (stable), aligns the members of each
  * cluster whose centroid passes the mode's gate (using d_shift if given, else
  * computing the shifts against d_centroids), re-z-normalises them, and replaces

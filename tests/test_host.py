@@ -17,7 +17,7 @@ def T(built):
 
 def header_symbols():
     text = open(os.path.join(ROOT, "include", "timesc.h")).read()
-    return sorted(set(re.findall(r"^\s*(?:int|void|const char\s*\*)\s+(tc_[a-z_0-9]+)\s*\(", text, re.M)))
+    return sorted(set(re.findall(r"^\s*(?:int|void|uint64_t|const char\s*\*)\s+(tc_[a-z_0-9]+)\s*\(", text, re.M)))
 
 
 def test_library_exports_every_declared_symbol(T):

@@ -409,3 +409,130 @@ void launch_init_labels(int32_t* labels, int64_t n, int k, cudaStream_t s) {
 }
 
 }  // namespace tc
+
+// ------------------------------------------------------------------ allocation-free assignment
+// tc_sbd_assign_noalloc: the same fused SBD assignment for callers that must not
+// allocate device memory on the call path (a serving loop that reserved all HBM
+// up front, or a thread that cannot take cudaMalloc's implicit synchronisation).
+// Its scratch (twiddle tables and centroid spectra) lives in one file-scope
+// device array instead of context buffers.  No counterpart in the reference.
+namespace tc {
+
+constexpr size_t NOALLOC_SCRATCH_BYTES = (size_t)4 << 20;  // TC_NOALLOC_SCRATCH_BYTES
+static __device__ __align__(256) float2 g_noalloc_scratch[NOALLOC_SCRATCH_BYTES / sizeof(float2)];
+
+struct NoallocDevice {
+    float2* scratch = nullptr;  // device address of g_noalloc_scratch on that device
+    int sm_count = 0;
+    size_t smem_optin = 0;
+};
+static std::mutex g_noalloc_mu;
+static NoallocDevice g_noalloc_dev[256];
+
+// Once per device, with that device current: the scratch array's device address
+// (a host-side reference to the symbol is not a device address).
+static NoallocDevice noalloc_setup(int dev) {
+    std::lock_guard<std::mutex> lock(g_noalloc_mu);
+    TC_REQUIRE(dev >= 0 && dev < 256, TC_ERR_ARG, "device index out of range");
+    NoallocDevice& d = g_noalloc_dev[dev];
+    if (!d.scratch) {
+        void* p = nullptr;
+        TC_CUDA(cudaGetSymbolAddress(&p, g_noalloc_scratch));
+        int sm = 0, optin = 0;
+        TC_CUDA(cudaDeviceGetAttribute(&sm, cudaDevAttrMultiProcessorCount, dev));
+        TC_CUDA(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
+        d.sm_count = sm;
+        d.smem_optin = (size_t)optin;
+        d.scratch = static_cast<float2*>(p);
+    }
+    return d;
+}
+
+// twN[e] = exp(-2 pi i e/N), twF[e] = exp(-2 pi i e/(2N)), e in [0, N)
+__global__ void k_noalloc_twiddles(float2* twN, float2* twF, int N) {
+    const int e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e < N) {
+        double s, c;
+        sincospi(-2.0 * (double)e / (double)N, &s, &c);
+        twN[e] = make_float2((float)c, (float)s);
+        sincospi(-(double)e / (double)N, &s, &c);
+        twF[e] = make_float2((float)c, (float)s);
+    }
+}
+
+template <int N>
+static void noalloc_n(const NoallocDevice& d, const float* x, const float* C, int64_t n, int m, int k, int F,
+                      int clamp2, int32_t* labels, float* dist, cudaStream_t s) {
+    float2* twN = d.scratch;
+    float2* twF = twN + N;
+    float2* spec = twF + N;
+    k_noalloc_twiddles<<<ceil_div(N, 256), 256, 0, s>>>(twN, twF, N);
+    TC_CHECK_LAUNCH();
+    const size_t ssm = Cfg<N>::BUF_BYTES + sizeof(TeamScratch);
+    TC_CUDA(cudaFuncSetAttribute(k_centroid_spectra<N>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ssm));
+    k_centroid_spectra<N><<<k, Plan<N>::T, ssm, s>>>(C, m, twN, twF, spec);
+    TC_CHECK_LAUNCH();
+    AssignParams p{};
+    p.x = x;
+    p.spec = spec;
+    p.twN = twN;
+    p.twF = twF;
+    p.n = n;
+    p.m = m;
+    p.k = k;
+    p.F = F;
+    p.clamp2 = clamp2;
+    p.labels = labels;
+    p.dist = dist;
+    const bool csmem = Cfg<N>::smem(k, true) <= d.smem_optin;
+    const size_t sm = Cfg<N>::smem(k, csmem);
+    auto fn = csmem ? k_assign_fft<N, true, false> : k_assign_fft<N, false, false>;
+    TC_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+    int per_sm = 0;
+    TC_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, Cfg<N>::BLOCK, sm));
+    const int64_t teams = (n + Cfg<N>::TEAMS - 1) / Cfg<N>::TEAMS;
+    const int grid = (int)std::min<int64_t>(teams, (int64_t)d.sm_count * std::max(per_sm, 1));
+    fn<<<grid, Cfg<N>::BLOCK, sm, s>>>(p);
+    TC_CHECK_LAUNCH();
+}
+
+}  // namespace tc
+
+extern "C" int tc_sbd_assign_noalloc(const float* d_x, const float* d_centroids, int64_t n, int m, int k, int mode,
+                                     int32_t* d_labels, float* d_dist, tc_stream stream, char* err, int err_len) {
+    using namespace tc;
+    auto fail = [&](int code, const std::string& msg) {
+        if (err && err_len > 0) std::snprintf(err, (size_t)err_len, "%s", msg.c_str());
+        return code;
+    };
+    try {
+        TC_REQUIRE(mode == TC_MODE_COMPAT || mode == TC_MODE_CANONICAL, TC_ERR_ARG, "unknown mode");
+        TC_REQUIRE(n >= 0 && n <= (int64_t)INT32_MAX, TC_ERR_ARG, "n must be in [0, 2^31)");
+        TC_REQUIRE(m >= 2 && m <= 8192, TC_ERR_UNSUPPORTED, "series length m must be in [2, 8192]");
+        TC_REQUIRE(k >= 1 && k <= 1024, TC_ERR_UNSUPPORTED, "k must be in [1, 1024]");
+        TC_REQUIRE((d_x && d_centroids && d_labels) || n == 0, TC_ERR_ARG, "null pointer");
+        const int F = fft_size(m, mode), N = F / 2;
+        TC_REQUIRE(F >= 8 && F <= 16384, TC_ERR_UNSUPPORTED, "FFT length outside [8, 16384]");
+        const size_t need = ((size_t)2 * N + (size_t)k * (N + 1)) * sizeof(float2);
+        TC_REQUIRE(need <= NOALLOC_SCRATCH_BYTES, TC_ERR_UNSUPPORTED,
+                   "scratch of " + std::to_string(need) + " bytes needed (2*(F/2) + k*(F/2+1) complex values), the "
+                   "static array holds " + std::to_string(NOALLOC_SCRATCH_BYTES));
+        int dev = 0;
+        TC_CUDA(cudaGetDevice(&dev));
+        const NoallocDevice d = noalloc_setup(dev);
+        if (n == 0) return TC_OK;
+        const int clamp2 = (mode == TC_MODE_COMPAT && 2 * m - 1 < 512) ? 1 : 0;
+        cudaStream_t s = (cudaStream_t)stream;
+        switch (N) {
+#define X(nn) \
+    case nn: noalloc_n<nn>(d, d_x, d_centroids, n, m, k, F, clamp2, d_labels, d_dist, s); break;
+            TC_FOR_EACH_N(X)
+#undef X
+            default:
+                return fail(TC_ERR_UNSUPPORTED, "FFT length not supported");
+        }
+        return TC_OK;
+    } catch (const TcError& e) {
+        return fail(e.code, e.msg);
+    }
+}

@@ -57,6 +57,7 @@ SIGNATURES = {
     "tc_znorm": (_int, [_vp, _vp, _i64, _int, _int, _vp]),
     "tc_init_labels": (_int, [_vp, _vp, _i64, _int, _vp]),
     "tc_sbd_assign": (_int, [_vp, _vp, _vp, _i64, _int, _int, _int, _int, _vp, _vp, _vp, _vp, _vp, _vp, _vp]),
+    "tc_sbd_assign_noalloc": (_int, [_vp, _vp, _i64, _int, _int, _int, _vp, _vp, _vp, ctypes.c_char_p, _int]),
     "tc_extract_shapes": (_int, [_vp, _vp, _vp, _vp, _vp, _i64, _int, _int, _int, _int, _int, _vp,
                                  ctypes.POINTER(_int), _vp]),
     "tc_kshape_run": (_int, [_vp, ctypes.POINTER(Job), ctypes.POINTER(Result)]),
@@ -178,6 +179,18 @@ class Context:
         self._check(lib().tc_kshape_run(self.h, ctypes.byref(job), ctypes.byref(res)))
         return dict(labels=labels, centroids=cents, iterations=res.iterations, sum_class=res.sum_class,
                     restarted=res.restarted, inertia=res.inertia, seconds=res.seconds)
+
+
+def sbd_assign_noalloc(x, C, labels, dist=None, mode=MODE_COMPAT, stream=None):
+    """Allocation-free SBD assignment (no context; scratch in a static device
+    array).  For callers that must not allocate device memory on the call path."""
+    n, m = x.shape
+    k = C.shape[0]
+    err = ctypes.create_string_buffer(256)
+    rc = lib().tc_sbd_assign_noalloc(_ptr(x), _ptr(C), n, m, k, mode, _ptr(labels), _ptr(dist), _stream(stream),
+                                     err, 256)
+    if rc != OK:
+        raise TimescError(rc, err.value.decode())
 
 
 # ---- host helpers
