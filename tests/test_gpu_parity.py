@@ -158,6 +158,25 @@ def test_extract_tensor_core_gram(gpu_ctx, mods, prec, tol, m, k, n):
     assert err < tol, err
 
 
+@pytest.mark.parametrize("m,k,n", [(512, 8, 4000), (2709, 3, 400)])
+def test_fp32_gram_3xtf32_matches_simt(gpu_ctx, mods, m, k, n, monkeypatch):
+    """The plain FP32 extraction's 3xTF32 tensor-core Gram against the SIMT FP32 Gram."""
+    import torch
+    T, O = mods
+    data, truth = make_data(T, n, m, k, seed=11 * m + k)
+    X = O.znorm(data.astype(np.float64)).astype(np.float32)
+    out = []
+    for simt in (False, True):
+        if simt:
+            monkeypatch.setenv("TIMESC_SIMT_GRAM", "1")
+        c = dev(np.zeros((k, m), np.float32))
+        gpu_ctx.extract_shapes(dev(X), dev(truth), c, mode=0)
+        torch.cuda.synchronize()
+        out.append(c.cpu().numpy())
+    monkeypatch.delenv("TIMESC_SIMT_GRAM", raising=False)
+    assert np.abs(out[0] - out[1]).max() < 2e-5
+
+
 def _cpu_labels_via_gpu_init(ctx, n, k):
     import torch
     t = torch.zeros(n, dtype=torch.int32, device="cuda")

@@ -18,6 +18,7 @@
 #include <cuda_bf16.h>
 
 #include <algorithm>
+#include <cstdlib>
 #include <vector>
 
 #include "sm100.cuh"
@@ -25,11 +26,20 @@
 
 namespace tc {
 
-constexpr int GT_STAGES = 4;
 constexpr int GT_TILE = 128;                       // rows per operand tile
 constexpr int GT_TILE_BYTES = GT_TILE * 128;       // 128 rows x 128 bytes
-constexpr int GT_SMEM = GT_STAGES * 2 * GT_TILE_BYTES + 1024;  // + alignment slack
 constexpr int GT_PAD = 64;                          // cluster K padding (elements)
+
+// FMT 1 = BF16, 2 = TF32, 3 = 3xTF32: x = hi + lo with hi, lo TF32, and
+// S = hi*hi + hi*lo + lo*hi (the dropped lo*lo is below FP32 rounding), FP32-class
+// products on the tensor cores for the plain FP32 form.
+template <int FMT>
+struct GtCfg {
+    static constexpr int TILES = FMT == 3 ? 4 : 2;  // operand tiles per stage
+    static constexpr int STAGES = FMT == 3 ? 3 : 4;
+    static constexpr int SMEM = STAGES * TILES * GT_TILE_BYTES + 1024;  // + alignment slack
+    static constexpr int KE = FMT == 1 ? 64 : 32;   // K elements per 128-byte slab
+};
 
 // ---------------------------------------------------------------- TMA descriptor
 typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
@@ -77,10 +87,11 @@ template <>
 __device__ __forceinline__ float convert_out<float>(float v) { return to_tf32(v); }
 
 // YT[a][p'] = seg[pos][a], p' = pos - offsets[c] + poff[c] for the cluster c holding pos.
+// With YTlo (3xTF32): YT gets tf32(x) and YTlo gets tf32(x - tf32(x)).
 template <class TO>
 __global__ void k_seg_transpose(const float* __restrict__ seg, int64_t n, int m, const int32_t* __restrict__ offsets,
                                 const int32_t* __restrict__ counts, const int64_t* __restrict__ poff, int k,
-                                TO* __restrict__ YT, int64_t Pp) {
+                                TO* __restrict__ YT, float* __restrict__ YTlo, int64_t Pp) {
     __shared__ float tile[32][33];
     const int tx = threadIdx.x, ty = threadIdx.y;
     const int64_t pos0 = (int64_t)blockIdx.x * 32;
@@ -105,18 +116,25 @@ __global__ void k_seg_transpose(const float* __restrict__ seg, int64_t n, int m,
 #pragma unroll
     for (int i = 0; i < 4; ++i) {
         const int a = a0 + ty + 8 * i;
-        if (a < m) YT[(int64_t)a * Pp + pp] = convert_out<TO>(tile[tx][ty + 8 * i]);
+        if (a < m) {
+            const float x = tile[tx][ty + 8 * i];
+            const TO hi = convert_out<TO>(x);
+            YT[(int64_t)a * Pp + pp] = hi;
+            if (YTlo) YTlo[(int64_t)a * Pp + pp] = to_tf32(x - (float)hi);
+        }
     }
 }
 
 // ---------------------------------------------------------------- Gram kernel
 template <int FMT>
 __global__ void __launch_bounds__(128, 1) k_gram_tc(const __grid_constant__ CUtensorMap tmap,
+                                                    const __grid_constant__ CUtensorMap tmap_lo,
                                                     const int32_t* __restrict__ counts,
                                                     const int64_t* __restrict__ poff, int m, int ld, int nt,
                                                     float* __restrict__ S, int* __restrict__ err) {
     extern __shared__ uint8_t smem_raw[];
-    __shared__ __align__(8) uint64_t full[GT_STAGES], empty[GT_STAGES], done;
+    typedef GtCfg<FMT> G;
+    __shared__ __align__(8) uint64_t full[G::STAGES], empty[G::STAGES], done;
     __shared__ uint32_t tmem_base;
     uint8_t* base = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
     const int c = blockIdx.y;
@@ -125,17 +143,18 @@ __global__ void __launch_bounds__(128, 1) k_gram_tc(const __grid_constant__ CUte
     int t = blockIdx.x, ta = 0;
     while (t >= nt - ta) { t -= nt - ta; ++ta; }
     const int tb = ta + t;
-    constexpr int KE = FMT == 2 ? 32 : 64;  // elements per 128-byte K slab
+    constexpr int KE = G::KE;
     const int nk = (cnt + KE - 1) / KE;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     if (threadIdx.x == 0) {
-        for (int s = 0; s < GT_STAGES; ++s) {
+        for (int s = 0; s < G::STAGES; ++s) {
             sm100::mbar_init(&full[s], 1);
             sm100::mbar_init(&empty[s], 1);
         }
         sm100::mbar_init(&done, 1);
         sm100::fence_mbar_init();
         sm100::prefetch_tmap(&tmap);
+        if (FMT == 3) sm100::prefetch_tmap(&tmap_lo);
     }
     if (warp == 0) {
         sm100::tmem_alloc(&tmem_base, 128);
@@ -150,28 +169,41 @@ __global__ void __launch_bounds__(128, 1) k_gram_tc(const __grid_constant__ CUte
     if (warp == 0 && lane == 0) {
         // TMA producer
         for (int kb = 0; kb < nk && ok; ++kb) {
-            const int s = kb % GT_STAGES, u = kb / GT_STAGES;
+            const int s = kb % G::STAGES, u = kb / G::STAGES;
             if (u > 0) ok = sm100::mbar_wait(&empty[s], (u - 1) & 1, err);
             if (!ok) break;
-            uint8_t* A = base + (size_t)s * 2 * GT_TILE_BYTES;
-            sm100::mbar_expect_tx(&full[s], 2 * GT_TILE_BYTES);
+            uint8_t* A = base + (size_t)s * G::TILES * GT_TILE_BYTES;  // [A | B | A_lo | B_lo]
+            sm100::mbar_expect_tx(&full[s], G::TILES * GT_TILE_BYTES);
             sm100::tma_load_2d(A, &tmap, x0 + kb * KE, ta * GT_TILE, &full[s]);
             sm100::tma_load_2d(A + GT_TILE_BYTES, &tmap, x0 + kb * KE, tb * GT_TILE, &full[s]);
+            if (FMT == 3) {
+                sm100::tma_load_2d(A + 2 * GT_TILE_BYTES, &tmap_lo, x0 + kb * KE, ta * GT_TILE, &full[s]);
+                sm100::tma_load_2d(A + 3 * GT_TILE_BYTES, &tmap_lo, x0 + kb * KE, tb * GT_TILE, &full[s]);
+            }
         }
     } else if (warp == 1 && lane == 0) {
         // MMA issuer
-        constexpr uint32_t ID = sm100::idesc(FMT, 128, 128);
+        constexpr uint32_t ID = sm100::idesc(FMT == 1 ? 1 : 2, 128, 128);
         for (int kb = 0; kb < nk && ok; ++kb) {
-            const int s = kb % GT_STAGES, u = kb / GT_STAGES;
+            const int s = kb % G::STAGES, u = kb / G::STAGES;
             ok = sm100::mbar_wait(&full[s], u & 1, err);
             if (!ok) break;
             sm100::tc_fence_after();
-            uint8_t* A = base + (size_t)s * 2 * GT_TILE_BYTES;
+            uint8_t* A = base + (size_t)s * G::TILES * GT_TILE_BYTES;
             const uint64_t da = sm100::desc_k_sw128(A), db = sm100::desc_k_sw128(A + GT_TILE_BYTES);
 #pragma unroll
             for (int kk = 0; kk < 4; ++kk) {  // 4 x 32 bytes of K per slab
-                if (FMT == 2) sm100::mma_tf32(tmem, da + 2 * kk, db + 2 * kk, ID, (kb | kk) != 0);
-                else sm100::mma_f16(tmem, da + 2 * kk, db + 2 * kk, ID, (kb | kk) != 0);
+                if (FMT == 1) {
+                    sm100::mma_f16(tmem, da + 2 * kk, db + 2 * kk, ID, (kb | kk) != 0);
+                } else {
+                    sm100::mma_tf32(tmem, da + 2 * kk, db + 2 * kk, ID, (kb | kk) != 0);
+                    if (FMT == 3) {
+                        const uint64_t dal = sm100::desc_k_sw128(A + 2 * GT_TILE_BYTES);
+                        const uint64_t dbl = sm100::desc_k_sw128(A + 3 * GT_TILE_BYTES);
+                        sm100::mma_tf32(tmem, da + 2 * kk, dbl + 2 * kk, ID, 1);
+                        sm100::mma_tf32(tmem, dal + 2 * kk, db + 2 * kk, ID, 1);
+                    }
+                }
             }
             sm100::mma_commit(&empty[s]);
         }
@@ -202,7 +234,7 @@ __global__ void __launch_bounds__(128, 1) k_gram_tc(const __grid_constant__ CUte
         }
     } else if (threadIdx.x == 0) {
         // the pipeline stopped early: let copies already issued land before the CTA leaves
-        for (int s = 0; s < GT_STAGES; ++s) sm100::mbar_wait(&full[s], 0, nullptr);
+        for (int s = 0; s < G::STAGES; ++s) sm100::mbar_wait(&full[s], 0, nullptr);
     }
     sm100::tc_fence_before();
     __syncthreads();
@@ -210,8 +242,10 @@ __global__ void __launch_bounds__(128, 1) k_gram_tc(const __grid_constant__ CUte
 }
 
 // ---------------------------------------------------------------- host
+// FP32 runs as 3xTF32 unless TIMESC_SIMT_GRAM is set (the SIMT kernel stays available).
 bool gram_tc_supported(int m, int precision) {
-    return (precision == TC_PREC_BF16 || precision == TC_PREC_TF32) && m >= 2;
+    if (precision == TC_PREC_FP32 && std::getenv("TIMESC_SIMT_GRAM")) return false;
+    return m >= 2;
 }
 
 void launch_gram_tc(tc_ctx* ctx, const float* seg, const int32_t* counts, const int32_t* offsets,
@@ -227,31 +261,37 @@ void launch_gram_tc(tc_ctx* ctx, const float* seg, const int32_t* counts, const 
     Pp = std::max<int64_t>(Pp, GT_PAD);
     int64_t* poff = ws.gram_poff.as<int64_t>(k);
     TC_CUDA(cudaMemcpyAsync(poff, hp.data(), sizeof(int64_t) * k, cudaMemcpyHostToDevice, s));
-    const bool tf32 = precision == TC_PREC_TF32;
-    const int esize = tf32 ? 4 : 2;
-    void* YT = ws.gram_yt.get((size_t)m * Pp * esize);
-    TC_CUDA(cudaMemsetAsync(YT, 0, (size_t)m * Pp * esize, s));
+    const int fmt = precision == TC_PREC_BF16 ? 1 : (precision == TC_PREC_TF32 ? 2 : 3);
+    const int esize = fmt == 1 ? 2 : 4;
+    const size_t plane = (size_t)m * Pp * esize;
+    char* YT = static_cast<char*>(ws.gram_yt.get(plane * (fmt == 3 ? 2 : 1)));
+    float* YTlo = fmt == 3 ? reinterpret_cast<float*>(YT + plane) : nullptr;
+    TC_CUDA(cudaMemsetAsync(YT, 0, plane * (fmt == 3 ? 2 : 1), s));
     dim3 tg(ceil_div(n, 32), ceil_div(m, 32)), tb(32, 8);
     if (n > 0) {
-        if (tf32)
-            k_seg_transpose<float><<<tg, tb, 0, s>>>(seg, n, m, offsets, counts, poff, k, (float*)YT, Pp);
-        else
+        if (fmt == 1)
             k_seg_transpose<__nv_bfloat16><<<tg, tb, 0, s>>>(seg, n, m, offsets, counts, poff, k,
-                                                             (__nv_bfloat16*)YT, Pp);
+                                                             (__nv_bfloat16*)YT, nullptr, Pp);
+        else
+            k_seg_transpose<float><<<tg, tb, 0, s>>>(seg, n, m, offsets, counts, poff, k, (float*)YT, YTlo, Pp);
         TC_CHECK_LAUNCH();
     }
-    CUtensorMap map = make_tmap_2d(YT, tf32 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT32 : CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, esize,
-                                   (uint64_t)m, (uint64_t)Pp, GT_TILE);
+    const CUtensorMapDataType dt = fmt == 1 ? CU_TENSOR_MAP_DATA_TYPE_BFLOAT16 : CU_TENSOR_MAP_DATA_TYPE_FLOAT32;
+    CUtensorMap map = make_tmap_2d(YT, dt, esize, (uint64_t)m, (uint64_t)Pp, GT_TILE);
+    CUtensorMap map_lo = fmt == 3 ? make_tmap_2d(YTlo, dt, esize, (uint64_t)m, (uint64_t)Pp, GT_TILE) : map;
     int* err = reinterpret_cast<int*>(ws.aux.as<char>(64) + 48);
     TC_CUDA(cudaMemsetAsync(err, 0, sizeof(int), s));
     const int nt = ceil_div(m, GT_TILE);
     dim3 grid(nt * (nt + 1) / 2, k);
-    if (tf32) {
-        TC_CUDA(cudaFuncSetAttribute(k_gram_tc<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, GT_SMEM));
-        k_gram_tc<2><<<grid, 128, GT_SMEM, s>>>(map, counts, poff, m, ld, nt, S, err);
+    if (fmt == 1) {
+        TC_CUDA(cudaFuncSetAttribute(k_gram_tc<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, GtCfg<1>::SMEM));
+        k_gram_tc<1><<<grid, 128, GtCfg<1>::SMEM, s>>>(map, map_lo, counts, poff, m, ld, nt, S, err);
+    } else if (fmt == 2) {
+        TC_CUDA(cudaFuncSetAttribute(k_gram_tc<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, GtCfg<2>::SMEM));
+        k_gram_tc<2><<<grid, 128, GtCfg<2>::SMEM, s>>>(map, map_lo, counts, poff, m, ld, nt, S, err);
     } else {
-        TC_CUDA(cudaFuncSetAttribute(k_gram_tc<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, GT_SMEM));
-        k_gram_tc<1><<<grid, 128, GT_SMEM, s>>>(map, counts, poff, m, ld, nt, S, err);
+        TC_CUDA(cudaFuncSetAttribute(k_gram_tc<3>, cudaFuncAttributeMaxDynamicSharedMemorySize, GtCfg<3>::SMEM));
+        k_gram_tc<3><<<grid, 128, GtCfg<3>::SMEM, s>>>(map, map_lo, counts, poff, m, ld, nt, S, err);
     }
     TC_CHECK_LAUNCH();
     int h_err = 0;
