@@ -121,6 +121,42 @@ class Clocks:
                 "reasons": reasons, "samples": len(rows)}
 
 
+def cufft_assign_ms(x, C, F, chunk=32768, reps=3):
+    """Library baseline (not the product): the reference's materialising NCC_3D +
+    get_pos_idx (ncc.cuh:469-517, kshape.cuh:35-96) in plain FP32 on cuFFT via
+    torch.fft, in chunks of series so the n*k*F spectra fit in memory.
+    Returns (ms per full assignment, labels)."""
+    import torch
+    n, m = x.shape
+    k = C.shape[0]
+    L = 2 * m - 1
+    slots = (torch.arange(L, device=x.device) - (m - 1)) % F
+    cn = torch.linalg.norm(C, dim=1)
+    Cs = torch.fft.rfft(C, n=F)
+    labels = torch.empty(n, dtype=torch.int64, device=x.device)
+
+    def run():
+        for i0 in range(0, n, chunk):
+            xs = x[i0:i0 + chunk]
+            xn = torch.linalg.norm(xs, dim=1)
+            P = torch.fft.rfft(xs, n=F)[:, None, :] * torch.conj(Cs)[None, :, :]
+            r = torch.fft.irfft(P, n=F)[:, :, slots]
+            den = xn[:, None] * cn[None, :]
+            den = torch.where(den == 0, torch.full_like(den, 1e10), den)
+            d = (1.0 - r / den[:, :, None]).amin(dim=2)
+            labels[i0:i0 + chunk] = d.argmin(dim=1)
+
+    run()
+    torch.cuda.synchronize()
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    a.record()
+    for _ in range(reps):
+        run()
+    b.record()
+    torch.cuda.synchronize()
+    return a.elapsed_time(b) / reps, labels
+
+
 def cpu_iteration(O, X, C, labels, mode, F, ns):
     m = X.shape[1]
     om = O.MODE_COMPAT if mode == 0 else O.MODE_CANONICAL
@@ -206,6 +242,7 @@ def main():
     ap.add_argument("--mode", default="compat", choices=sorted(MODES))
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-cufft", action="store_true")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     wl = WORKLOADS[args.workload]
@@ -309,6 +346,15 @@ def main():
                "kshape_iters_per_s": 1e3 / ms_step,
                "assign_pairs_per_s": n * k / (a_ms / 1e3),
                "roofline": roof, "gpu_launches": int(launches), "clocks": clocks}
+
+    # library baseline: the reference's cuFFT formulation in plain FP32
+    if out is not None and not args.no_cufft:
+        cu_ms, cu_lab = cufft_assign_ms(x, C, F)
+        agree = float((cu_lab.to(torch.int32) == labels).float().mean().item())
+        out["plain_fp32_cufft"] = {"assign_pairs_per_s": n * k / (cu_ms / 1e3), "ms": cu_ms,
+                                   "label_agreement_with_fused": agree,
+                                   "what": "materialising NCC_3D + get_pos_idx on cuFFT (torch.fft), FP32, chunked"}
+        out["fused_vs_cufft_assign_speedup"] = cu_ms / a_ms
 
     # end-to-end through the public C ABI with pinned host buffers
     if not args.no_e2e:

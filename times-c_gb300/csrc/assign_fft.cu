@@ -64,12 +64,21 @@ struct TeamScratch {
     int u[16];
 };
 
-// Sum over the team; every thread gets the result.
+// Sum over the team (compensated FP32 within warps, FP64 across warps); every
+// thread gets the result.
 template <int T>
-__device__ __forceinline__ double team_sum(double v, int team, int tid, TeamScratch* scr) {
+__device__ __forceinline__ double team_sum(float x, int team, int tid, TeamScratch* scr) {
     constexpr int W = T < 32 ? T : 32;
+    float s = x, c = 0.f;  // value = s - c
 #pragma unroll
-    for (int o = W / 2; o > 0; o >>= 1) v += __shfl_xor_sync(team_mask<T>(), v, o, W);
+    for (int o = W / 2; o > 0; o >>= 1) {
+        const float s2 = __shfl_xor_sync(team_mask<T>(), s, o, W), c2 = __shfl_xor_sync(team_mask<T>(), c, o, W);
+        const float t = s + s2, bp = t - s;
+        const float err = (s - (t - bp)) + (s2 - bp);
+        s = t;
+        c = c + c2 - err;
+    }
+    double v = (double)s - (double)c;
     if constexpr (T > 32) {
         if ((tid & 31) == 0) scr->sum[tid >> 5] = v;
         team_sync<T>(team);
@@ -136,7 +145,7 @@ __device__ __forceinline__ void forward_row(const float* __restrict__ x, int m, 
     typedef Core<N> C;
     float2 v[2][C::R0];
     float ss = C::fwd_load(x, m, tid, v);
-    nrm2 = team_sum<C::T>((double)ss, team, tid, scr);
+    nrm2 = team_sum<C::T>(ss, team, tid, scr);
     C::template pass0_store<false>(v, tid, buf);
     team_sync<C::T>(team);
     NoOut no;

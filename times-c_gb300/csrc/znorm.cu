@@ -38,6 +38,30 @@ __device__ __forceinline__ RowSrc row_source(const float* src, int64_t row, int 
     return r;
 }
 
+// Compensated FP32 sums: Kahan within a lane, TwoSum across lanes; every lane
+// gets the total.  (GB300 retires few FP64 lane-operations per clock, so the
+// per-row path stays in FP32.)
+struct KSum {
+    float s = 0.f, c = 0.f;  // value = s - c
+    __device__ __forceinline__ void add(float x) {
+        const float y = x - c, t = s + y;
+        c = (t - s) - y;
+        s = t;
+    }
+};
+__device__ __forceinline__ float warp_sum_comp(KSum k) {
+    float s = k.s, c = k.c;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        const float s2 = __shfl_xor_sync(0xffffffffu, s, o), c2 = __shfl_xor_sync(0xffffffffu, c, o);
+        const float t = s + s2, bp = t - s;
+        const float err = (s - (t - bp)) + (s2 - bp);
+        s = t;
+        c = c + c2 - err;
+    }
+    return s - c;
+}
+
 template <int VPL, bool GATHER>
 __global__ void __launch_bounds__(256) k_norm_rows_warp(const float* __restrict__ src, float* dst, int64_t n, int m,
                                                         int ddof, const int32_t* __restrict__ perm,
@@ -50,25 +74,26 @@ __global__ void __launch_bounds__(256) k_norm_rows_warp(const float* __restrict_
     for (int64_t row = w0; row < n; row += nw) {
         RowSrc rs = row_source<GATHER>(src, row, m, perm, labels, shift, gate);
         float v[VPL];
-        float s = 0.f;
+        KSum s;
 #pragma unroll
         for (int q = 0; q < VPL; ++q) {
             int t = lane + 32 * q;
             int a = t - rs.shift;
             v[q] = (t < m && a >= 0 && a < m) ? rs.x[a] : 0.f;
-            s += v[q];
+            s.add(v[q]);
         }
-        const float mean = (float)(warp_sum_d((double)s) / m);
-        float ss = 0.f;
+        const float mean = warp_sum_comp(s) / (float)m;
+        KSum ss;
 #pragma unroll
         for (int q = 0; q < VPL; ++q) {
             int t = lane + 32 * q;
             float d = t < m ? v[q] - mean : 0.f;
             v[q] = d;
-            ss += d * d;
+            ss.add(d * d);
         }
-        const double sd = sqrt(warp_sum_d((double)ss) / (double)(m - ddof));
-        const float inv = (sd > 0.0 && isfinite(sd)) ? (float)(1.0 / sd) : 0.f;
+        const float var = warp_sum_comp(ss) / (float)(m - ddof);
+        const float sd = sqrtf(var);
+        const float inv = (sd > 0.f && isfinite(sd)) ? 1.0f / sd : 0.f;
         float* y = dst + (size_t)row * m;
 #pragma unroll
         for (int q = 0; q < VPL; ++q) {
