@@ -53,9 +53,11 @@ typedef enum {
 } tc_mode;
 
 typedef enum {
-    TC_PREC_FP32 = 0,      /* SIMT FP32 FFT correlation */
-    TC_PREC_BF16 = 1,      /* tensor-core (tcgen05) correlation, BF16 operands, FP32 accumulation */
-    TC_PREC_TF32 = 2       /* tensor-core (tcgen05) correlation, TF32 operands, FP32 accumulation */
+    TC_PREC_FP32 = 0,      /* FP32 FFT correlation; Gram matrices in 3xTF32 on the tensor cores */
+    TC_PREC_BF16 = 1,      /* BF16 operands, FP32 accumulation, on the tensor cores (tcgen05): the
+                              correlation when FFT length is 128..1024 (m <= 512) and no shift is
+                              requested (the FP32 FFT correlation otherwise), and the Gram matrices */
+    TC_PREC_TF32 = 2       /* TF32 Gram matrices on the tensor cores; FP32 FFT correlation */
 } tc_precision;
 
 /* ---------------------------------------------------------------- context */

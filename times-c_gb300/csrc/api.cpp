@@ -57,17 +57,14 @@ static void assign(tc_ctx* ctx, const float* x, const float* C, int64_t n, int m
     a.old_labels = old;
     a.changed = changed;
     a.dist_sum = dsum;
-    if (precision == TC_PREC_FP32) {
+    if (precision == TC_PREC_FP32 || shift || !tc_assign_supported(m, F, k, precision)) {
         float2* spec = ctx->ws.spectra.as<float2>((size_t)k * (F / 2 + 1));
         launch_centroid_spectra(ctx, C, k, m, F, spec, s);
         a.spec = spec;
         launch_assign_fft(ctx, a, s);
     } else {
-        TC_REQUIRE(tc_assign_supported(m, F, k, precision), TC_ERR_UNSUPPORTED,
-                   "tensor-core correlation does not support this shape/precision; use TC_PREC_FP32");
-        a.spec = nullptr;
+        a.centroids = C;
         launch_assign_tc(ctx, a, precision, s);
-        (void)C;
     }
 }
 
@@ -237,7 +234,7 @@ int tc_destroy(tc_ctx* ctx) {
                       &ctx->ws.centroids, &ctx->ws.spectra, &ctx->ws.seg, &ctx->ws.perm, &ctx->ws.chunk_counts,
                       &ctx->ws.counts, &ctx->ws.offsets, &ctx->ws.gate, &ctx->ws.scal, &ctx->ws.gram,
                       &ctx->ws.rowsum, &ctx->ws.gram_yt, &ctx->ws.gram_poff, &ctx->ws.piter, &ctx->ws.pstats, &ctx->ws.aux, &ctx->ws.toeplitz,
-                      &ctx->ws.xbf};
+                      &ctx->ws.toeplitz_norm, &ctx->ws.xbf, &ctx->ws.xbf_norm};
     for (DevBuf* b : bufs) b->release();
     for (auto* t : ctx->fft) {
         t->twN.release();

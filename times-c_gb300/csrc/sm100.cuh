@@ -61,6 +61,13 @@ __device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* map, i
         "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(smem_u32(bar))
         : "memory");
 }
+// Untiled bulk copy global -> shared (both 16-byte aligned, bytes a multiple of 16).
+__device__ __forceinline__ void bulk_load(void* dst, const void* src, uint32_t bytes, uint64_t* bar) {
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                     smem_u32(dst)),
+                 "l"(reinterpret_cast<uint64_t>(src)), "r"(bytes), "r"(smem_u32(bar))
+                 : "memory");
+}
 __device__ __forceinline__ void prefetch_tmap(const CUtensorMap* map) {
     asm volatile("prefetch.tensormap [%0];" ::"l"(reinterpret_cast<uint64_t>(map)) : "memory");
 }
@@ -134,6 +141,21 @@ __device__ __forceinline__ uint64_t desc_k_sw128(const void* base) {
     d |= (uint64_t)(1024 >> 4) << 32;        // stride byte offset: 8 rows * 128 B
     d |= 1ull << 46;                         // descriptor version (sm100)
     d |= 2ull << 61;                         // SWIZZLE_128B
+    return d;
+}
+
+// K-major operand without swizzle: core matrices of 8 rows x 16 bytes, rows 16
+// bytes apart; lbo = byte distance between core matrices along K, sbo = along
+// M/N.  With lbo = 16 and sbo = 128 the core matrices overlap and row n, element
+// k reads base[8n + k] (16-bit elements): a Toeplitz operand straight from one
+// shifted copy of a sequence.
+__device__ __forceinline__ uint64_t desc_k_none(const void* base, uint32_t lbo, uint32_t sbo) {
+    const uint64_t addr = smem_u32(base);
+    uint64_t d = 0;
+    d |= (addr & 0x3FFFFull) >> 4;
+    d |= (uint64_t)(lbo >> 4) << 16;
+    d |= (uint64_t)(sbo >> 4) << 32;
+    d |= 1ull << 46;  // descriptor version (sm100); layout type 0 = no swizzle
     return d;
 }
 

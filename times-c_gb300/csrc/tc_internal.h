@@ -88,7 +88,9 @@ struct Workspace {
     DevBuf pstats;       // 3*k*4 f64
     DevBuf aux;          // small scalars (changed count, dist sum, sum_class, flags)
     DevBuf toeplitz;     // bf16 shifted centroid copies for the tensor-core correlation
+    DevBuf toeplitz_norm;  // k f32 centroid norms
     DevBuf xbf;          // bf16 copy of the series for the tensor-core correlation
+    DevBuf xbf_norm;     // n f32 series norms
 };
 
 struct tc_ctx {
@@ -114,7 +116,8 @@ void launch_centroid_spectra(tc_ctx* ctx, const float* C, int k, int m, int F, f
 
 struct AssignArgs {
     const float* x;
-    const float2* spec;        // k*(N+1)
+    const float* centroids;    // k*m (tensor-core correlation)
+    const float2* spec;        // k*(N+1) (FFT correlation)
     int64_t n;
     int m, k, F;
     int clamp2;                // pad value 2 of get_pos_idx (compat, 2m-1 < 512)

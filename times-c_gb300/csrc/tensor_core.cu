@@ -1,5 +1,4 @@
-// Tensor-core (tcgen05) Gram matrices for the mixed-precision extraction, and
-// (not yet built) the tensor-core correlation.
+// Tensor-core (tcgen05) Gram matrices for the shape extraction.
 //
 // S_c = Y_c^T Y_c (shapeExtract.cuh:532-537, a cuBLAS SGEMM per cluster with
 // k CUDA streams in the reference) becomes one launch over all clusters and the
@@ -59,7 +58,7 @@ static EncodeTiledFn encode_fn() {
 }
 
 // 2-D row-major tensor [rows][cols] of esize-byte elements; box = 128 bytes x box_rows.
-static CUtensorMap make_tmap_2d(const void* base, CUtensorMapDataType dt, int esize, uint64_t rows, uint64_t cols,
+CUtensorMap make_tmap_2d(const void* base, CUtensorMapDataType dt, int esize, uint64_t rows, uint64_t cols,
                                 uint32_t box_rows) {
     CUtensorMap map;
     cuuint64_t dims[2] = {cols, rows};
@@ -298,12 +297,6 @@ void launch_gram_tc(tc_ctx* ctx, const float* seg, const int32_t* counts, const 
     TC_CUDA(cudaMemcpyAsync(&h_err, err, sizeof(int), cudaMemcpyDeviceToHost, s));
     TC_CUDA(cudaStreamSynchronize(s));
     TC_REQUIRE(h_err == 0, TC_ERR_TIMEOUT, "tensor-core Gram: a pipeline wait ran out");
-}
-
-// ---------------------------------------------------------------- correlation (not built yet)
-bool tc_assign_supported(int, int, int, int) { return false; }
-void launch_assign_tc(tc_ctx*, const AssignArgs&, int, cudaStream_t) {
-    throw TcError{TC_ERR_UNSUPPORTED, "tensor-core correlation not built"};
 }
 
 }  // namespace tc
