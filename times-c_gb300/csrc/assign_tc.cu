@@ -5,21 +5,25 @@
 // The circular correlation at lag t of the zero-padded length F is
 //   r[t] = sum_{u < m} x[u] * c_pad[(u - t) mod F],
 // a GEMM of the series (M = series, K = samples) with a Toeplitz matrix
-// (N = lags).  The Toeplitz operand is never built: for b in 0..7 one shifted
-// copy buf_b[e] = c_pad[(e - b) mod F] of the centroid is enough, because a
-// K-major no-swizzle UMMA descriptor with 16-byte core-matrix strides (LBO 16,
-// SBO 128) reads row n, element u from buf_b[8n + u] - row n is lag b - 8n.
-// Eight copies (F/8 rows each) cover all F lags.
+// (N = lags).  The Toeplitz operand is never built.  A K-major, no-swizzle UMMA
+// descriptor reads 8-row core matrices whose rows are 16 bytes (8 elements)
+// apart; with LBO = 16 bytes, row r of a core matrix reads q = 8r + u of one
+// buffer, and SBO (the distance between 8-row groups) is set to the length of
+// a buffer, so each 8-row group reads its own buffer.  Buffer G holds the
+// centroid shifted by T_G = 64 (G / 8) + G % 8, buf_G[q] = c_pad[(q - T_G) mod F],
+// and its rows give the 8 lags T_G - 8r; the F/8 buffers cover every lag once.
+// One MMA takes 32 buffers: N = 256 lags per instruction (F/8 buffers, N = F,
+// when F = 128), the shape at which the tensor core runs at full rate.
 //
 // Persistent, warp-specialised CTA (192 threads), one per SM:
-//   warp 0  producer: TMA of a 128-series BF16 tile (resident for all
-//           centroids) and bulk copies of each centroid's 8 shifted copies into a
-//           double buffer;
-//   warp 1  one thread issues M=128, N=F/8, K=16 MMAs into two 256-column TMEM
-//           slots (b-groups of 256 lags), so MMAs fill one slot while the
-//           epilogue drains the other;
+//   warp 0  producer: TMA of a 128-series BF16 tile (resident in shared memory
+//           for all centroids) and bulk copies of 32-buffer groups into a
+//           two-stage ring;
+//   warp 1  one thread issues M=128, N=256, K=16 MMAs into two 256-column TMEM
+//           accumulator slots, so MMAs fill one slot while the epilogue drains
+//           the other;
 //   warps 2-5 epilogue: tcgen05.ld of the row's 256 lags, max over valid lags,
-//           NCC = max / (|x||c|) with FP32 norms of the original data, and the
+//           NCC = max / (|x||c|) with FP32 norms of the unrounded data, and the
 //           running argmin over centroids - only (label, distance) reach HBM.
 // All waits are bounded and report through an error word.
 #include <cuda.h>
@@ -41,30 +45,35 @@ constexpr int AT_TILE = 128;        // series per tile (UMMA M)
 constexpr int AT_SLOT_COLS = 256;   // TMEM columns per accumulator slot
 
 struct AtGeom {
-    int m, mp, F, NB, lnb, Gb, G, KS, Lb, bsz, nch;
-    // mp: padded K (multiple of 64), NB = F/8 lags per shifted copy, Gb copies per
-    // TMEM slot, G groups, KS = mp/16 K steps, Lb = elements per copy, bsz = bytes
-    // of one centroid's 8 copies, nch = 64-column chunks of the series tile
+    int m, mp, F, NBT, CPG, NG, H, KS, Lq, gsz, nch;
+    // mp: padded K (multiple of 64); NBT = F/8 shifted buffers per centroid; CPG
+    // buffers per MMA group, NG = 8*CPG lags per MMA (N), H groups per centroid;
+    // KS = mp/16 K steps; Lq = elements per buffer (reads reach 8*7 + mp - 1);
+    // gsz = bytes of one group; nch = 64-column chunks of the series tile
     __host__ __device__ AtGeom(int m_, int F_) : m(m_), F(F_) {
         mp = (m + 63) / 64 * 64;
-        NB = F / 8;
-        lnb = 0;
-        while ((1 << lnb) < NB) ++lnb;
-        Gb = AT_SLOT_COLS / NB < 8 ? AT_SLOT_COLS / NB : 8;
-        G = 8 / Gb;
+        NBT = F / 8;
+        CPG = NBT < 32 ? NBT : 32;
+        NG = 8 * CPG;
+        H = NBT / CPG;
         KS = mp / 16;
-        Lb = (F + mp + 7) / 8 * 8;
-        bsz = 8 * Lb * 2;
+        Lq = mp + 56;
+        gsz = CPG * Lq * 2;
         nch = mp / 64;
     }
     // at least 116 KB so that one CTA (and one 512-column TMEM allocation) fits an SM
     size_t smem() const {
-        const size_t s = (size_t)nch * 16384 + 2 * (size_t)bsz + 1024;
+        const size_t s = (size_t)nch * 16384 + 2 * (size_t)gsz + 1024;
         return s > 116 * 1024 ? s : 116 * 1024;
     }
 };
 
-// Series -> BF16 [n][mp] (zero padded) and FP32 norms (compensated).
+// lag of buffer G's row r: T_G - 8r (mod F)
+__host__ __device__ inline int at_lag(int G, int r, int F) { return (64 * (G >> 3) + (G & 7) - 8 * r) & (F - 1); }
+
+// Series -> BF16 [n][mp] (zero padded) and FP32 norms (compensated), one warp
+// per row; V4: rows of float4 (m % 4 == 0 and a 16-byte aligned base).
+template <bool V4>
 __global__ void k_series_bf16(const float* __restrict__ x, int64_t n, int m, int mp, __nv_bfloat16* __restrict__ xb,
                               float* __restrict__ xnorm) {
     const int lane = threadIdx.x & 31;
@@ -74,12 +83,31 @@ __global__ void k_series_bf16(const float* __restrict__ x, int64_t n, int m, int
         const float* r = x + (size_t)i * m;
         __nv_bfloat16* o = xb + (size_t)i * mp;
         float s = 0.f, c = 0.f;
-        for (int t = lane; t < mp; t += 32) {
-            const float v = t < m ? r[t] : 0.f;
-            o[t] = __float2bfloat16_rn(v);
+        auto acc = [&](float v) {
             const float y = v * v - c, tt = s + y;
             c = (tt - s) - y;
             s = tt;
+        };
+        if constexpr (V4) {
+            for (int t = lane; t < mp / 4; t += 32) {
+                float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
+                if (4 * t < m) v = __ldg(reinterpret_cast<const float4*>(r) + t);
+                acc(v.x);
+                acc(v.y);
+                acc(v.z);
+                acc(v.w);
+                __nv_bfloat162 lo = __floats2bfloat162_rn(v.x, v.y), hi = __floats2bfloat162_rn(v.z, v.w);
+                uint2 pk;
+                pk.x = *reinterpret_cast<uint32_t*>(&lo);
+                pk.y = *reinterpret_cast<uint32_t*>(&hi);
+                reinterpret_cast<uint2*>(o)[t] = pk;
+            }
+        } else {
+            for (int t = lane; t < mp; t += 32) {
+                const float v = t < m ? r[t] : 0.f;
+                o[t] = __float2bfloat16_rn(v);
+                acc(v);
+            }
         }
         double d = (double)s - (double)c;
 #pragma unroll
@@ -88,8 +116,9 @@ __global__ void k_series_bf16(const float* __restrict__ x, int64_t n, int m, int
     }
 }
 
-// Centroid j -> 8 shifted BF16 copies buf_b[e] = c_pad[(e - b) mod F], e < Lb, and its norm.
-__global__ void k_centroid_toeplitz(const float* __restrict__ C, int m, int F, int Lb,
+// Centroid j -> F/8 shifted BF16 buffers buf_G[q] = c_pad[(q - T_G) mod F], q < Lq,
+// and its norm.
+__global__ void k_centroid_toeplitz(const float* __restrict__ C, int m, int F, int Lq,
                                     __nv_bfloat16* __restrict__ B, float* __restrict__ cnorm) {
     __shared__ double red[32];
     const int j = blockIdx.x;
@@ -105,20 +134,21 @@ __global__ void k_centroid_toeplitz(const float* __restrict__ C, int m, int F, i
         for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += red[w];
         cnorm[j] = (float)sqrt(t);
     }
-    __nv_bfloat16* o = B + (size_t)j * 8 * Lb;
-    for (int e = threadIdx.x; e < 8 * Lb; e += blockDim.x) {
-        const int b = e / Lb, q = e % Lb;
-        const int u = ((q - b) % F + F) % F;
+    const int nb = F / 8;
+    __nv_bfloat16* o = B + (size_t)j * nb * Lq;
+    for (int e = threadIdx.x; e < nb * Lq; e += blockDim.x) {
+        const int G = e / Lq, q = e % Lq;
+        const int u = (q - at_lag(G, 0, F)) & (F - 1);
         o[e] = __float2bfloat16_rn(u < m ? c[u] : 0.f);
     }
 }
 
 struct AtParams {
-    const __nv_bfloat16* B;  // [k][8][Lb]
+    const __nv_bfloat16* B;  // [k][F/8][Lq] shifted buffers
     const float* xnorm;
     const float* cnorm;
     int64_t n;
-    int m, k, F, clamp2, mask;
+    int m, k, F, clamp2;
     int32_t* labels;
     float* dist;
     const int32_t* old_labels;
@@ -131,10 +161,11 @@ __global__ void __launch_bounds__(AT_THREADS, 1) k_assign_tc(const __grid_consta
     extern __shared__ uint8_t smem_raw[];
     __shared__ __align__(8) uint64_t a_full, a_empty, b_full[2], b_empty[2], t_full[2], t_empty[2], fin;
     __shared__ uint32_t tmem_base;
+    __shared__ uint32_t lagmask[32];  // valid-lag bits per (group, 32-column chunk)
     const AtGeom g(p.m, p.F);
     uint8_t* base = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
     uint8_t* Atile = base;                                    // nch x 16 KB, 128B-swizzled K-major
-    uint8_t* Bslot = base + (size_t)g.nch * 16384;            // 2 x bsz
+    uint8_t* Bring = base + (size_t)g.nch * 16384;            // 2 x gsz
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int64_t ntiles = (p.n + AT_TILE - 1) / AT_TILE;
     if (threadIdx.x == 0) {
@@ -150,6 +181,18 @@ __global__ void __launch_bounds__(AT_THREADS, 1) k_assign_tc(const __grid_consta
         sm100::fence_mbar_init();
         sm100::prefetch_tmap(&tmapX);
     }
+    if (threadIdx.x < 32) {
+        // column col of group h is row col of the MMA: buffer h*CPG + col/8, row col%8.
+        // Valid lags are t <= m-1 and t >= F-m+1 (all of them when F <= 2m-1).
+        const int h = threadIdx.x >> 3, ch = threadIdx.x & 7;
+        uint32_t bits = 0;
+        for (int e = 0; e < 32; ++e) {
+            const int col = ch * 32 + e;
+            const int t = at_lag(h * g.CPG + (col >> 3), col & 7, g.F);
+            if (col < g.NG && (t <= p.m - 1 || t >= g.F - p.m + 1)) bits |= 1u << e;
+        }
+        lagmask[threadIdx.x] = bits;
+    }
     if (warp == 0) {
         sm100::tmem_alloc(&tmem_base, 2 * AT_SLOT_COLS);
         sm100::tmem_relinquish();
@@ -164,63 +207,64 @@ __global__ void __launch_bounds__(AT_THREADS, 1) k_assign_tc(const __grid_consta
         if (lane == 0) {  // producer
             int64_t q = 0;
             int lt = 0;
+            const size_t cent = (size_t)g.NBT * g.Lq;  // elements per centroid
             for (int64_t tile = blockIdx.x; tile < ntiles && ok; tile += gridDim.x, ++lt) {
                 if (lt > 0) ok = sm100::mbar_wait(&a_empty, (lt - 1) & 1, p.err);
                 if (!ok) break;
                 sm100::mbar_expect_tx(&a_full, (uint32_t)g.nch * 16384);
                 for (int c = 0; c < g.nch; ++c)
                     sm100::tma_load_2d(Atile + (size_t)c * 16384, &tmapX, 64 * c, (int)(tile * AT_TILE), &a_full);
-                for (int j = 0; j < p.k; ++j, ++q) {
-                    const int s = (int)(q & 1), u = (int)(q >> 1);
-                    if (u > 0) ok = sm100::mbar_wait(&b_empty[s], (u - 1) & 1, p.err);
-                    if (!ok) break;
-                    sm100::mbar_expect_tx(&b_full[s], (uint32_t)g.bsz);
-                    sm100::bulk_load(Bslot + (size_t)s * g.bsz, p.B + (size_t)j * 8 * g.Lb, (uint32_t)g.bsz, &b_full[s]);
-                }
+                for (int j = 0; j < p.k && ok; ++j)
+                    for (int h = 0; h < g.H; ++h, ++q) {
+                        const int s = (int)(q & 1), u = (int)(q >> 1);
+                        if (u > 0) ok = sm100::mbar_wait(&b_empty[s], (u - 1) & 1, p.err);
+                        if (!ok) break;
+                        sm100::mbar_expect_tx(&b_full[s], (uint32_t)g.gsz);
+                        sm100::bulk_load(Bring + (size_t)s * g.gsz, p.B + j * cent + (size_t)h * g.CPG * g.Lq,
+                                         (uint32_t)g.gsz, &b_full[s]);
+                    }
             }
             // copies still in flight land before the CTA can exit: wait for the last
             // phase issued on each barrier (already complete on the normal path)
             if (lt > 0) sm100::mbar_wait(&a_full, (lt - 1) & 1, p.err);
             for (int s = 0; s < 2; ++s) {
-                const int64_t uses = (q + 1 - s) / 2;  // loads issued into slot s
+                const int64_t uses = (q + 1 - s) / 2;  // loads issued into stage s
                 if (uses > 0) sm100::mbar_wait(&b_full[s], (int)((uses - 1) & 1), p.err);
             }
         }
         __syncwarp();
     } else if (warp == 1) {
         if (lane == 0) {  // MMA issuer
-            const uint32_t ID = sm100::idesc(1, AT_TILE, g.NB);
-            int64_t q = 0, w = 0;
+            const uint32_t ID = sm100::idesc(1, AT_TILE, g.NG);
+            // descriptors advance by adding to their 14-bit address field (bytes >> 4):
+            // +2 per 16 K elements, +1024 per 16 KB A chunk, gsz/16 per ring stage
+            const uint64_t da0 = sm100::desc_k_sw128(Atile);
+            const uint64_t db0 = sm100::desc_k_none(Bring, 16, (uint32_t)g.Lq * 2);
+            int64_t q = 0;
             int lt = 0;
             for (int64_t tile = blockIdx.x; tile < ntiles && ok; tile += gridDim.x, ++lt) {
                 ok = sm100::mbar_wait(&a_full, lt & 1, p.err);
                 if (!ok) break;
                 sm100::tc_fence_after();
-                for (int j = 0; j < p.k && ok; ++j, ++q) {
-                    const int s = (int)(q & 1);
-                    ok = sm100::mbar_wait(&b_full[s], (int)(q >> 1) & 1, p.err);
-                    if (!ok) break;
-                    sm100::tc_fence_after();
-                    const uint8_t* Bs = Bslot + (size_t)s * g.bsz;
-                    for (int gi = 0; gi < g.G && ok; ++gi, ++w) {
-                        const int s2 = (int)(w & 1);
-                        if (w >= 2) ok = sm100::mbar_wait(&t_empty[s2], (int)((w >> 1) - 1) & 1, p.err);
+                for (int j = 0; j < p.k && ok; ++j)
+                    for (int h = 0; h < g.H; ++h, ++q) {
+                        // ring stage and accumulator slot both follow the group counter
+                        const int s = (int)(q & 1);
+                        ok = sm100::mbar_wait(&b_full[s], (int)(q >> 1) & 1, p.err);
+                        if (ok && q >= 2) ok = sm100::mbar_wait(&t_empty[s], (int)((q >> 1) - 1) & 1, p.err);
                         if (!ok) break;
                         sm100::tc_fence_after();
-                        for (int bb = 0; bb < g.Gb; ++bb) {
-                            const int b = gi * g.Gb + bb;
-                            const uint32_t d = tmem + s2 * AT_SLOT_COLS + bb * g.NB;
-                            const uint8_t* buf = Bs + (size_t)b * g.Lb * 2;
-                            for (int kk = 0; kk < g.KS; ++kk) {
-                                const uint64_t da = sm100::desc_k_sw128(Atile + (size_t)(kk >> 2) * 16384) + 2 * (kk & 3);
-                                const uint64_t db = sm100::desc_k_none(buf + 32 * kk, 16, 128);
-                                sm100::mma_f16(d, da, db, ID, kk > 0);
-                            }
+                        const uint32_t d = tmem + s * AT_SLOT_COLS;
+                        const uint64_t db = db0 + (uint64_t)((s * g.gsz) >> 4);
+                        for (int kc = 0; kc < g.nch; ++kc) {
+                            const uint64_t da = da0 + (uint64_t)(kc * 1024);
+#pragma unroll
+                            for (int u = 0; u < 4; ++u)
+                                sm100::mma_f16(d, da + 2 * u, db + 2 * (4 * kc + u), ID, (kc | u) != 0);
                         }
-                        sm100::mma_commit(&t_full[s2]);
+                        sm100::mma_commit(&t_full[s]);
+                        sm100::mma_commit(&b_empty[s]);
                     }
-                    sm100::mma_commit(&b_empty[s]);
-                }
                 sm100::mma_commit(&a_empty);
             }
             // every MMA issued completes before TMEM is released
@@ -232,10 +276,11 @@ __global__ void __launch_bounds__(AT_THREADS, 1) k_assign_tc(const __grid_consta
         // epilogue: TMEM lane quarter warp%4 = series rows 32*(warp%4) + lane
         const int quarter = warp & 3;
         const int row = quarter * 32 + lane;
+        const uint32_t tq = tmem + ((uint32_t)(quarter * 32) << 16);
+        const int nchunk = g.NG / 32;  // 4 or 8
         double dsum = 0.0;
         int nchg = 0;
-        int64_t w = 0;
-        const int slot_chunks = (g.Gb * g.NB) / 32;
+        int64_t q = 0;
         for (int64_t tile = blockIdx.x; tile < ntiles && ok; tile += gridDim.x) {
             const int64_t i = tile * AT_TILE + row;
             const float xn = i < p.n ? p.xnorm[i] : 0.f;
@@ -243,31 +288,34 @@ __global__ void __launch_bounds__(AT_THREADS, 1) k_assign_tc(const __grid_consta
             int bestj = 0;
             for (int j = 0; j < p.k && ok; ++j) {
                 float mx = -3.0e38f;
-                for (int gi = 0; gi < g.G && ok; ++gi, ++w) {
-                    const int s2 = (int)(w & 1);
-                    ok = __all_sync(0xffffffffu, sm100::mbar_wait(&t_full[s2], (int)(w >> 1) & 1, p.err));
+                for (int h = 0; h < g.H && ok; ++h, ++q) {
+                    const int s = (int)(q & 1);
+                    ok = __all_sync(0xffffffffu, sm100::mbar_wait(&t_full[s], (int)(q >> 1) & 1, p.err));
                     if (!ok) break;
                     sm100::tc_fence_after();
-                    for (int ch = 0; ch < slot_chunks; ++ch) {
-                        float r[32];
-                        sm100::tmem_ld32(tmem + ((uint32_t)(quarter * 32) << 16) + s2 * AT_SLOT_COLS + ch * 32, r);
+                    for (int c0 = 0; c0 < nchunk; c0 += 4) {
+                        float r[4][32];
+#pragma unroll
+                        for (int ch = 0; ch < 4; ++ch)
+                            sm100::tmem_ld32(tq + s * AT_SLOT_COLS + (c0 + ch) * 32, r[ch]);
                         sm100::tmem_ld_wait();
-                        if (!p.mask) {
+                        if (c0 + 4 >= nchunk) {  // the slot is free once its last columns are in registers
+                            sm100::tc_fence_before();
+                            __syncwarp();
+                            if (lane == 0) sm100::mbar_arrive(&t_empty[s]);
+                        }
 #pragma unroll
-                            for (int e = 0; e < 32; ++e) mx = fmaxf(mx, r[e]);
-                        } else {
+                        for (int ch = 0; ch < 4; ++ch) {
+                            const uint32_t vm = lagmask[h * 8 + c0 + ch];  // bit e: column valid
+                            float m0 = -3.0e38f, m1 = -3.0e38f;
 #pragma unroll
-                            for (int e = 0; e < 32; ++e) {
-                                const int col = ch * 32 + e;
-                                const int b = gi * g.Gb + (col >> g.lnb), nn = col & (g.NB - 1);
-                                const int t = (b - 8 * nn) & (g.F - 1);  // lag of this column
-                                if (t <= p.m - 1 || t >= g.F - p.m + 1) mx = fmaxf(mx, r[e]);
+                            for (int e = 0; e < 32; e += 2) {
+                                m0 = fmaxf(m0, (vm >> e) & 1u ? r[ch][e] : -3.0e38f);
+                                m1 = fmaxf(m1, (vm >> (e + 1)) & 1u ? r[ch][e + 1] : -3.0e38f);
                             }
+                            mx = fmaxf(mx, fmaxf(m0, m1));
                         }
                     }
-                    sm100::tc_fence_before();
-                    __syncwarp();
-                    if (lane == 0) sm100::mbar_arrive(&t_empty[s2]);
                 }
                 const float den = xn * p.cnorm[j];
                 const float ncc = den > 0.f ? mx / den : 0.f;  // a zero norm gives NCC 0 (ncc.cuh:89)
@@ -313,12 +361,15 @@ void launch_assign_tc(tc_ctx* ctx, const AssignArgs& a, int precision, cudaStrea
     TC_REQUIRE(g.smem() <= ctx->smem_optin, TC_ERR_UNSUPPORTED, "tensor-core correlation: shared memory");
     __nv_bfloat16* xb = ws.xbf.as<__nv_bfloat16>((size_t)a.n * g.mp);
     float* xnorm = ws.xbf_norm.as<float>((size_t)a.n);
-    __nv_bfloat16* B = ws.toeplitz.as<__nv_bfloat16>((size_t)a.k * 8 * g.Lb);
+    __nv_bfloat16* B = ws.toeplitz.as<__nv_bfloat16>((size_t)a.k * g.NBT * g.Lq);
     float* cnorm = ws.toeplitz_norm.as<float>((size_t)a.k);
     const int wgrid = (int)std::min<int64_t>(ceil_div(a.n, 8), (int64_t)ctx->sm_count * 16);
-    k_series_bf16<<<wgrid, 256, 0, s>>>(a.x, a.n, a.m, g.mp, xb, xnorm);
+    if (a.m % 4 == 0 && reinterpret_cast<uintptr_t>(a.x) % 16 == 0)
+        k_series_bf16<true><<<wgrid, 256, 0, s>>>(a.x, a.n, a.m, g.mp, xb, xnorm);
+    else
+        k_series_bf16<false><<<wgrid, 256, 0, s>>>(a.x, a.n, a.m, g.mp, xb, xnorm);
     TC_CHECK_LAUNCH();
-    k_centroid_toeplitz<<<a.k, 256, 0, s>>>(a.centroids, a.m, a.F, g.Lb, B, cnorm);
+    k_centroid_toeplitz<<<a.k, 256, 0, s>>>(a.centroids, a.m, a.F, g.Lq, B, cnorm);
     TC_CHECK_LAUNCH();
     CUtensorMap map = make_tmap_2d(xb, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, (uint64_t)a.n, (uint64_t)g.mp, AT_TILE);
     int* err = reinterpret_cast<int*>(ws.aux.as<char>(64) + 52);
@@ -332,7 +383,6 @@ void launch_assign_tc(tc_ctx* ctx, const AssignArgs& a, int precision, cudaStrea
     p.k = a.k;
     p.F = a.F;
     p.clamp2 = a.clamp2;
-    p.mask = a.F >= 2 * a.m ? 1 : 0;  // lags m..F-m fall outside the 2m-1 valid ones
     p.labels = a.labels;
     p.dist = a.dist;
     p.old_labels = a.old_labels;
