@@ -95,6 +95,14 @@ int tc_sbd_assign(tc_ctx* ctx, const float* d_x, const float* d_centroids, int64
                   const int32_t* d_old_labels, int32_t* d_changed, double* d_dist_sum,
                   tc_stream stream);
 
+/* Keeps a BF16 copy of the series d_x (n rows of length m <= 512) and their FP32
+ * norms in the context for the tensor-core correlation: later tc_sbd_assign calls
+ * with TC_PREC_BF16 and the same d_x, n and m use it instead of converting the
+ * series again.  The copy is taken now: call again after changing d_x.  Any
+ * tc_sbd_assign on other series, and tc_kshape_run, drop it.  No counterpart in
+ * the reference (NCC_3D transforms the series on every iteration). */
+int tc_prepare_series(tc_ctx* ctx, const float* d_x, int64_t n, int m, tc_stream stream);
+
 /* Allocation-free SBD assignment.  No counterpart in the reference.
  * For callers that must not allocate device memory on the call path: a serving
  * loop that reserved all HBM for resident jobs up front, or a latency-critical

@@ -137,3 +137,34 @@ def test_tc_kshape_loop_bf16(gpu_ctx, mods_tc, mode):
 @pytest.fixture(scope="module")
 def mods_tc(built):
     return built
+
+
+def test_tc_prepared_series(gpu_ctx, mods_tc):
+    """Assignments on prepared series match unprepared ones; assigning other
+    series in between drops the prepared copy instead of reusing it."""
+    import torch
+    T, O = mods_tc
+    n, m, k = 3000, 256, 5
+    d1, _ = T.generate(n, m, k, noise=0.3, seed=21)
+    d2, _ = T.generate(n, m, k, noise=0.3, seed=22)
+    x1 = dev(O.znorm(d1.astype(np.float64)).astype(np.float32))
+    x2 = dev(O.znorm(d2.astype(np.float64)).astype(np.float32))
+    c = x1[:k].clone()
+
+    def run(x):
+        lab = torch.zeros(n, dtype=torch.int32, device="cuda")
+        dist = torch.zeros(n, dtype=torch.float32, device="cuda")
+        gpu_ctx.sbd_assign(x, c, mode=1, precision=T.PREC_BF16, labels=lab, dist=dist)
+        torch.cuda.synchronize()
+        return lab.cpu().numpy(), dist.cpu().numpy()
+
+    ref1, ref2 = run(x1), run(x2)
+    gpu_ctx.prepare_series(x1)
+    for _ in range(2):
+        a = run(x1)
+        assert np.array_equal(a[0], ref1[0]) and np.array_equal(a[1], ref1[1])
+    b = run(x2)
+    assert np.array_equal(b[1], ref2[1])
+    x1.mul_(-1.0)  # changed after its copy was dropped: the next call converts again
+    a = run(x1)
+    assert not np.array_equal(a[1], ref1[1])

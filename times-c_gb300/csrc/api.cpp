@@ -289,6 +289,16 @@ int tc_sbd_assign(tc_ctx* ctx, const float* d_x, const float* d_centroids, int64
     TC_API_END(ctx)
 }
 
+int tc_prepare_series(tc_ctx* ctx, const float* d_x, int64_t n, int m, tc_stream stream) {
+    if (!ctx) return TC_ERR_ARG;
+    TC_API_BEGIN
+    TC_REQUIRE(n >= 0 && m >= 2 && m <= 512, TC_ERR_ARG, "tc_prepare_series: n >= 0 and 2 <= m <= 512");
+    TC_REQUIRE(d_x || n == 0, TC_ERR_ARG, "null pointer");
+    TC_CUDA(cudaSetDevice(ctx->device));
+    prepare_series_bf16(ctx, d_x, n, m, (cudaStream_t)stream);
+    TC_API_END(ctx)
+}
+
 int tc_extract_shapes(tc_ctx* ctx, const float* d_x, const int32_t* d_labels, const int32_t* d_shift,
                       float* d_centroids, int64_t n, int m, int k, int mode, int cal_select, int precision,
                       int32_t* d_counts, int* h_sum_class, tc_stream stream) {
@@ -341,6 +351,9 @@ int tc_kshape_run(tc_ctx* ctx, const tc_job* job, tc_result* res) {
     else
         TC_CUDA(cudaMemcpyAsync(x, job->d_data, sizeof(float) * n * m, cudaMemcpyDeviceToDevice, s));
     launch_znorm(x, n, m, 1, ctx->sm_count, s);  // test_kshape.cu:37 / :99
+    // the series stay fixed for the whole run: their BF16 copy is made once
+    if (job->precision != TC_PREC_FP32 && tc_assign_supported(m, fft_size(m, job->mode), k, job->precision))
+        prepare_series_bf16(ctx, x, n, m, s);
     const int cap = job->max_iter > 0 ? job->max_iter : 20;
     LoopState st = run_loop(ctx, job, x, k, job->init_chose == 1, 0, cap, s);
     res->restarted = 0;
@@ -355,6 +368,7 @@ int tc_kshape_run(tc_ctx* ctx, const tc_job* job, tc_result* res) {
         TC_CUDA(cudaMemcpyAsync(res->h_centroids, ctx->ws.centroids.p, sizeof(float) * k * m, cudaMemcpyDeviceToHost,
                                 s));
     TC_CUDA(cudaStreamSynchronize(s));
+    ctx->prep_x = nullptr;
     res->iterations = st.iterations;
     res->sum_class = st.sum_class;
     res->inertia = st.inertia;

@@ -349,6 +349,24 @@ __global__ void __launch_bounds__(AT_THREADS, 1) k_assign_tc(const __grid_consta
 }
 
 // ---------------------------------------------------------------- host
+void prepare_series_bf16(tc_ctx* ctx, const float* x, int64_t n, int m, cudaStream_t s) {
+    const int mp = (m + 63) / 64 * 64;
+    __nv_bfloat16* xb = ctx->ws.xbf.as<__nv_bfloat16>((size_t)n * mp);
+    float* xnorm = ctx->ws.xbf_norm.as<float>((size_t)n);
+    ctx->prep_x = nullptr;
+    if (n > 0) {
+        const int wgrid = (int)std::min<int64_t>(ceil_div(n, 8), (int64_t)ctx->sm_count * 16);
+        if (m % 4 == 0 && reinterpret_cast<uintptr_t>(x) % 16 == 0)
+            k_series_bf16<true><<<wgrid, 256, 0, s>>>(x, n, m, mp, xb, xnorm);
+        else
+            k_series_bf16<false><<<wgrid, 256, 0, s>>>(x, n, m, mp, xb, xnorm);
+        TC_CHECK_LAUNCH();
+    }
+    ctx->prep_x = x;
+    ctx->prep_n = n;
+    ctx->prep_m = m;
+}
+
 bool tc_assign_supported(int m, int F, int k, int precision) {
     return precision == TC_PREC_BF16 && m >= 2 && m <= 512 && F >= 128 && F <= 1024 && k >= 1;
 }
@@ -359,16 +377,14 @@ void launch_assign_tc(tc_ctx* ctx, const AssignArgs& a, int precision, cudaStrea
     Workspace& ws = ctx->ws;
     const AtGeom g(a.m, a.F);
     TC_REQUIRE(g.smem() <= ctx->smem_optin, TC_ERR_UNSUPPORTED, "tensor-core correlation: shared memory");
+    if (!(ctx->prep_x == a.x && ctx->prep_n == a.n && ctx->prep_m == a.m)) {
+        prepare_series_bf16(ctx, a.x, a.n, a.m, s);
+        ctx->prep_x = nullptr;  // converted for this call only: the caller may change x
+    }
     __nv_bfloat16* xb = ws.xbf.as<__nv_bfloat16>((size_t)a.n * g.mp);
     float* xnorm = ws.xbf_norm.as<float>((size_t)a.n);
     __nv_bfloat16* B = ws.toeplitz.as<__nv_bfloat16>((size_t)a.k * g.NBT * g.Lq);
     float* cnorm = ws.toeplitz_norm.as<float>((size_t)a.k);
-    const int wgrid = (int)std::min<int64_t>(ceil_div(a.n, 8), (int64_t)ctx->sm_count * 16);
-    if (a.m % 4 == 0 && reinterpret_cast<uintptr_t>(a.x) % 16 == 0)
-        k_series_bf16<true><<<wgrid, 256, 0, s>>>(a.x, a.n, a.m, g.mp, xb, xnorm);
-    else
-        k_series_bf16<false><<<wgrid, 256, 0, s>>>(a.x, a.n, a.m, g.mp, xb, xnorm);
-    TC_CHECK_LAUNCH();
     k_centroid_toeplitz<<<a.k, 256, 0, s>>>(a.centroids, a.m, a.F, g.Lq, B, cnorm);
     TC_CHECK_LAUNCH();
     CUtensorMap map = make_tmap_2d(xb, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, (uint64_t)a.n, (uint64_t)g.mp, AT_TILE);

@@ -64,7 +64,8 @@ __device__ __forceinline__ double rsqrt_d(double x) {
     return y;
 }
 
-template <int CL>
+// BPL > 0: rows of at most 32*BPL float4 (loads unrolled); 0: any length.
+template <int CL, int BPL>
 __global__ void __launch_bounds__(PC_THREADS) k_power_cluster(PowerClusterParams p) {
     namespace cg = cooperative_groups;
     cg::cluster_group cluster = cg::this_cluster();
@@ -134,37 +135,60 @@ __global__ void __launch_bounds__(PC_THREADS) k_power_cluster(PowerClusterParams
     int T = p.tmax;
     const float4* v4 = reinterpret_cast<const float4*>(v);
     const int nv4 = ld / 4;
+    constexpr int U = BPL >= 8 ? 2 : PC_UNROLL;  // rows in flight per warp
     for (int t = 0;; ++t) {
         const int par = t & 1;
         const float cr = sh_corr[0], cc = sh_corr[1];
         double acc[4] = {0.0, 0.0, 0.0, 0.0};
-        for (int i0 = wid * PC_UNROLL; i0 < nrow; i0 += nw * PC_UNROLL) {
-            float s[PC_UNROLL], cp[PC_UNROLL];
-            const float4* rowp[PC_UNROLL];
+        for (int i0 = wid * U; i0 < nrow; i0 += nw * U) {
+            float s[U], cp[U];
+            const float4* rowp[U];
 #pragma unroll
-            for (int u = 0; u < PC_UNROLL; ++u) {
+            for (int u = 0; u < U; ++u) {
                 s[u] = 0.f;
                 cp[u] = 0.f;
                 rowp[u] = reinterpret_cast<const float4*>(Sc + (size_t)(a0 + min(i0 + u, nrow - 1)) * ld);
             }
-            for (int b = lane; b < nv4; b += 32) {
-                const float4 w = v4[b];
-                float4 x[PC_UNROLL];
+            auto kahan4 = [&](int u, const float4& x, const float4& w) {
+                const float pr[4] = {x.x * w.x, x.y * w.y, x.z * w.z, x.w * w.w};
 #pragma unroll
-                for (int u = 0; u < PC_UNROLL; ++u) x[u] = __ldg(rowp[u] + b);
+                for (int e = 0; e < 4; ++e) {
+                    const float yk = pr[e] - cp[u], tt = s[u] + yk;
+                    cp[u] = (tt - s[u]) - yk;
+                    s[u] = tt;
+                }
+            };
+            if constexpr (BPL > 0) {
+                // every load of the U rows in flight at once: one L2 round trip per step
+                float4 x[U][BPL];
 #pragma unroll
-                for (int u = 0; u < PC_UNROLL; ++u) {
-                    const float pr[4] = {x[u].x * w.x, x[u].y * w.y, x[u].z * w.z, x[u].w * w.w};
+                for (int u = 0; u < U; ++u)
 #pragma unroll
-                    for (int e = 0; e < 4; ++e) {  // Kahan
-                        const float yk = pr[e] - cp[u], tt = s[u] + yk;
-                        cp[u] = (tt - s[u]) - yk;
-                        s[u] = tt;
+                    for (int j = 0; j < BPL; ++j) {
+                        const int b = lane + 32 * j;
+                        x[u][j] = b < nv4 ? __ldg(rowp[u] + b) : make_float4(0.f, 0.f, 0.f, 0.f);
                     }
+#pragma unroll
+                for (int j = 0; j < BPL; ++j) {
+                    const int b = lane + 32 * j;
+                    if (b < nv4) {
+                        const float4 w = v4[b];
+#pragma unroll
+                        for (int u = 0; u < U; ++u) kahan4(u, x[u][j], w);
+                    }
+                }
+            } else {
+                for (int b = lane; b < nv4; b += 32) {
+                    const float4 w = v4[b];
+                    float4 x[U];
+#pragma unroll
+                    for (int u = 0; u < U; ++u) x[u] = __ldg(rowp[u] + b);
+#pragma unroll
+                    for (int u = 0; u < U; ++u) kahan4(u, x[u], w);
                 }
             }
 #pragma unroll
-            for (int u = 0; u < PC_UNROLL; ++u) {
+            for (int u = 0; u < U; ++u) {
 #pragma unroll
                 for (int o = 16; o > 0; o >>= 1) {
                     const float s2 = __shfl_xor_sync(0xffffffffu, s[u], o);
@@ -285,10 +309,11 @@ __global__ void __launch_bounds__(PC_THREADS) k_power_cluster(PowerClusterParams
 }
 
 // ---------------------------------------------------------------- host
-template <int CL>
+template <int CL, int BPL>
 static void launch_cluster(const PowerClusterParams& pp, int k, size_t smem, cudaStream_t s) {
-    TC_CUDA(cudaFuncSetAttribute(k_power_cluster<CL>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    if (CL > 8) TC_CUDA(cudaFuncSetAttribute(k_power_cluster<CL>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
+    auto kern = k_power_cluster<CL, BPL>;
+    TC_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    if (CL > 8) TC_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3((unsigned)k * CL);
     cfg.blockDim = dim3(PC_THREADS);
@@ -301,7 +326,7 @@ static void launch_cluster(const PowerClusterParams& pp, int k, size_t smem, cud
     attr[0].val.clusterDim.z = 1;
     cfg.attrs = attr;
     cfg.numAttrs = 1;
-    TC_CUDA(cudaLaunchKernelEx(&cfg, k_power_cluster<CL>, pp));
+    TC_CUDA(cudaLaunchKernelEx(&cfg, kern, pp));
     TC_CHECK_LAUNCH();
 }
 
@@ -322,9 +347,14 @@ void power_eigvecs(tc_ctx* ctx, const float* S, int ld, const double* r, const d
     if (m > 1024) {
         const size_t smem = cluster_smem<16>(m, ld);
         TC_REQUIRE(smem + 4096 <= ctx->smem_optin, TC_ERR_UNSUPPORTED, "power iteration: series too long");
-        launch_cluster<16>(pp, k, smem, s);
+        launch_cluster<16, 0>(pp, k, smem, s);
     } else {
-        launch_cluster<8>(pp, k, cluster_smem<8>(m, ld), s);
+        const int nv4 = ld / 4;
+        const size_t smem = cluster_smem<8>(m, ld);
+        if (nv4 <= 32) launch_cluster<8, 1>(pp, k, smem, s);
+        else if (nv4 <= 64) launch_cluster<8, 2>(pp, k, smem, s);
+        else if (nv4 <= 128) launch_cluster<8, 4>(pp, k, smem, s);
+        else launch_cluster<8, 8>(pp, k, smem, s);
     }
     if (std::getenv("TIMESC_TRACE")) {
         std::vector<int> h(k);

@@ -101,6 +101,10 @@ struct tc_ctx {
     std::vector<FftTables*> fft;  // cached per F
     Workspace ws;
     cudaStream_t own_stream = nullptr;
+    // series whose BF16 copy and norms sit in ws.xbf / ws.xbf_norm (tc_prepare_series)
+    const float* prep_x = nullptr;
+    int64_t prep_n = 0;
+    int prep_m = 0;
 };
 
 namespace tc {
@@ -134,6 +138,8 @@ void launch_assign_fft(tc_ctx* ctx, const AssignArgs& a, cudaStream_t s);
 // tensor-core correlation (tcgen05); returns false when the shape is not supported
 bool tc_assign_supported(int m, int F, int k, int precision);
 void launch_assign_tc(tc_ctx* ctx, const AssignArgs& a, int precision, cudaStream_t s);
+// BF16 copy and norms of the series into the context's workspace, marked as prepared for x
+void prepare_series_bf16(tc_ctx* ctx, const float* x, int64_t n, int m, cudaStream_t s);
 
 // extraction
 struct ExtractArgs {

@@ -57,6 +57,7 @@ SIGNATURES = {
     "tc_znorm": (_int, [_vp, _vp, _i64, _int, _int, _vp]),
     "tc_init_labels": (_int, [_vp, _vp, _i64, _int, _vp]),
     "tc_sbd_assign": (_int, [_vp, _vp, _vp, _i64, _int, _int, _int, _int, _vp, _vp, _vp, _vp, _vp, _vp, _vp]),
+    "tc_prepare_series": (_int, [_vp, _vp, _i64, _int, _vp]),
     "tc_sbd_assign_noalloc": (_int, [_vp, _vp, _i64, _int, _int, _int, _vp, _vp, _vp, ctypes.c_char_p, _int]),
     "tc_extract_shapes": (_int, [_vp, _vp, _vp, _vp, _vp, _i64, _int, _int, _int, _int, _int, _vp,
                                  ctypes.POINTER(_int), _vp]),
@@ -151,6 +152,11 @@ class Context:
         self._check(lib().tc_sbd_assign(self.h, _ptr(x), _ptr(C), n, m, k, mode, precision, _ptr(labels),
                                         _ptr(dist), _ptr(shift), _ptr(old_labels), _ptr(changed),
                                         _ptr(dist_sum), _stream(stream)))
+
+    def prepare_series(self, x, stream=None):
+        """Keep a BF16 copy of x for TC_PREC_BF16 assignments on the same tensor."""
+        n, m = x.shape
+        self._check(lib().tc_prepare_series(self.h, _ptr(x), n, m, _stream(stream)))
 
     def extract_shapes(self, x, labels, C, shift=None, mode=MODE_COMPAT, cal_select=0, precision=PREC_FP32,
                        counts=None, stream=None):
