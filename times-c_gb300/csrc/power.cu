@@ -15,8 +15,10 @@
 // stop independently.  Rank 0 finishes: Rayleigh quotient, sign rule, store.
 //
 // Arithmetic: row dot products are compensated FP32 (Kahan per lane, TwoSum
-// across lanes); the norm, the sums and the step difference are accumulated in
-// FP64, so rounding noise in |v_t - v_{t-1}| stays well below the tolerance.
+// across lanes); the norm, the sums and the step difference are accumulated as
+// FP32 pairs (TwoSum, products split exactly by FMA: about 44 bits), so rounding
+// noise in |v_t - v_{t-1}| stays well below the tolerance; FP64 only for the
+// final per-step norm and corrections (one thread).
 #include <cooperative_groups.h>
 
 #include <algorithm>
@@ -66,7 +68,7 @@ __device__ __forceinline__ double rsqrt_d(double x) {
 
 // BPL > 0: rows of at most 32*BPL float4 (loads unrolled); 0: any length.
 template <int CL, int BPL>
-__global__ void __launch_bounds__(PC_THREADS) k_power_cluster(PowerClusterParams p) {
+__global__ void __launch_bounds__(PC_THREADS, 1) k_power_cluster(PowerClusterParams p) {
     namespace cg = cooperative_groups;
     cg::cluster_group cluster = cg::this_cluster();
     extern __shared__ __align__(16) unsigned char dsm[];
@@ -80,10 +82,11 @@ __global__ void __launch_bounds__(PC_THREADS) k_power_cluster(PowerClusterParams
     auto a16 = [](size_t x) { return (x + 15) & ~size_t(15); };
     float* v = reinterpret_cast<float*>(dsm);
     float* ybuf = reinterpret_cast<float*>(dsm + a16((size_t)ld * 4));
-    double* part = reinterpret_cast<double*>(dsm + a16((size_t)ld * 4) + a16((size_t)2 * ld * 4));
+    float2* part = reinterpret_cast<float2*>(dsm + a16((size_t)ld * 4) + a16((size_t)2 * ld * 4));
     float* vprev = reinterpret_cast<float*>(reinterpret_cast<unsigned char*>(part) + a16((size_t)2 * CL * 4 * 8));
     float* r_own = vprev + a16((size_t)nrow * 4) / 4;
     __shared__ double red[PC_THREADS / 32][4];
+    __shared__ float2 red2[PC_THREADS / 32][4];  // per-step partials
     __shared__ float sh_corr[2];
     __shared__ double sh_inv;
     __shared__ int sh_done;
@@ -125,7 +128,7 @@ __global__ void __launch_bounds__(PC_THREADS) k_power_cluster(PowerClusterParams
         __syncthreads();
     }
     float* yrem[CL];
-    double* prem[CL];
+    float2* prem[CL];
 #pragma unroll
     for (int q = 0; q < CL; ++q) {
         yrem[q] = cluster.map_shared_rank(ybuf, q);
@@ -139,7 +142,13 @@ __global__ void __launch_bounds__(PC_THREADS) k_power_cluster(PowerClusterParams
     for (int t = 0;; ++t) {
         const int par = t & 1;
         const float cr = sh_corr[0], cc = sh_corr[1];
-        double acc[4] = {0.0, 0.0, 0.0, 0.0};
+        // per-step sums as FP32 pairs (value = s - c), exact products by FMA: GB300's
+        // FP64 pipe is too narrow for per-row double arithmetic
+        float accs[4] = {0.f, 0.f, 0.f, 0.f}, accc[4] = {0.f, 0.f, 0.f, 0.f};
+        auto add_prod = [&](int q, float a, float b) {
+            const float pr = a * b, e = fmaf(a, b, -pr);  // a*b = pr + e exactly
+            two_sum_acc(accs[q], accc[q], pr, -e);
+        };
         for (int i0 = wid * U; i0 < nrow; i0 += nw * U) {
             float s[U], cp[U];
             const float4* rowp[U];
@@ -202,13 +211,13 @@ __global__ void __launch_bounds__(PC_THREADS) k_power_cluster(PowerClusterParams
                     const float yf = (s[u] - cp[u]) + fmaf(cr, ra, cc);
                     if (lane < CL) yrem[lane][par * ld + a] = yf;  // into every CTA of the cluster
                     if (lane == 0) {
-                        acc[0] = fma((double)yf, (double)yf, acc[0]);
-                        acc[1] += (double)yf;
-                        acc[2] = fma((double)ra, (double)yf, acc[2]);
+                        add_prod(0, yf, yf);
+                        two_sum_acc(accs[1], accc[1], yf, 0.f);
+                        add_prod(2, ra, yf);
                         const float va = v[a];
                         if (t >= 1) {
                             const float d = va - vprev[i];
-                            acc[3] = fma((double)d, (double)d, acc[3]);
+                            add_prod(3, d, d);
                         }
                         vprev[i] = va;
                     }
@@ -216,21 +225,24 @@ __global__ void __launch_bounds__(PC_THREADS) k_power_cluster(PowerClusterParams
             }
         }
         if (lane == 0)
-            for (int q = 0; q < 4; ++q) red[wid][q] = acc[q];
+            for (int q = 0; q < 4; ++q) red2[wid][q] = make_float2(accs[q], accc[q]);
         __syncthreads();
         if (threadIdx.x < 4) {
-            double sum = 0;
-            for (int w = 0; w < nw; ++w) sum += red[w][threadIdx.x];
+            float ss = 0.f, sc = 0.f;
+            for (int w = 0; w < nw; ++w) two_sum_acc(ss, sc, red2[w][threadIdx.x].x, red2[w][threadIdx.x].y);
 #pragma unroll
-            for (int q = 0; q < CL; ++q) prem[q][(par * CL + rank) * 4 + threadIdx.x] = sum;
+            for (int q = 0; q < CL; ++q) prem[q][(par * CL + rank) * 4 + threadIdx.x] = make_float2(ss, sc);
         }
         cluster.sync();  // y and partials of step t visible in every CTA
         if (threadIdx.x == 0) {  // identical in every CTA (rank order)
-            double n2 = 0, sy = 0, ry = 0, dd = 0;
+            float ts[4] = {0.f, 0.f, 0.f, 0.f}, tcm[4] = {0.f, 0.f, 0.f, 0.f};
             for (int q = 0; q < CL; ++q) {
-                const double* pq = part + (par * CL + q) * 4;
-                n2 += pq[0]; sy += pq[1]; ry += pq[2]; dd += pq[3];
+                const float2* pq = part + (par * CL + q) * 4;
+#pragma unroll
+                for (int e = 0; e < 4; ++e) two_sum_acc(ts[e], tcm[e], pq[e].x, pq[e].y);
             }
+            const double n2 = (double)ts[0] - (double)tcm[0], sy = (double)ts[1] - (double)tcm[1];
+            const double ry = (double)ts[2] - (double)tcm[2], dd = (double)ts[3] - (double)tcm[3];
             const double inv = rsqrt_d(n2), sv = sy * inv, rv = ry * inv;
             sh_corr[0] = (float)(-sv * inv_m);
             sh_corr[1] = (float)(-rv * inv_m + totc * sv * inv_m * inv_m);
