@@ -2,6 +2,7 @@
 #include <algorithm>
 #include <chrono>
 #include <cmath>
+#include <cstdlib>
 #include <cstring>
 #include <new>
 
@@ -68,6 +69,71 @@ static void assign(tc_ctx* ctx, const float* x, const float* C, int64_t n, int m
     }
 }
 
+// Error words the asynchronous stages leave in aux: Gram at +48, tensor-core
+// correlation at +52.
+static void check_async_errors(const int* words) {
+    TC_REQUIRE(words[0] == 0, TC_ERR_TIMEOUT, "tensor-core Gram: a pipeline wait ran out");
+    TC_REQUIRE(words[1] == 0, TC_ERR_TIMEOUT, "tensor-core correlation: a pipeline wait ran out");
+}
+
+// One stage of an iteration (extraction, or assignment) as a CUDA graph: the
+// first run issues the launches directly (workspace buffers, FFT tables and
+// kernel attributes get set up), the second captures them and later runs replay
+// the graph.  The stages hold no host synchronisation, and their buffers and
+// arguments are the same every iteration.  If capture or instantiation fails
+// the stage keeps issuing its launches directly.
+struct StageGraph {
+    cudaGraphExec_t exec = nullptr;
+    bool warm = false, failed = false;
+    uint64_t kernels = 0;  // kernel launches recorded in the graph
+    StageGraph() = default;
+    StageGraph(const StageGraph&) = delete;
+    StageGraph& operator=(const StageGraph&) = delete;
+    ~StageGraph() {
+        if (exec) cudaGraphExecDestroy(exec);
+    }
+    template <class F>
+    void run(bool enabled, cudaStream_t s, F&& issue) {
+        if (!enabled || failed || !warm) {
+            issue();
+            warm = true;
+            return;
+        }
+        if (!exec) capture(s, issue);
+        if (exec) {
+            TC_CUDA(cudaGraphLaunch(exec, s));
+            g_launches.fetch_add(kernels, std::memory_order_relaxed);  // the kernels the replay runs
+        } else {
+            issue();
+        }
+    }
+    template <class F>
+    void capture(cudaStream_t s, F&& issue) {
+        cudaGraph_t gr = nullptr;
+        if (cudaStreamBeginCapture(s, cudaStreamCaptureModeRelaxed) != cudaSuccess) {
+            cudaGetLastError();
+            failed = true;
+            return;
+        }
+        bool ok = true;
+        const uint64_t before = g_launches.load();
+        try {
+            issue();
+        } catch (const TcError&) {
+            ok = false;
+        }
+        kernels = g_launches.load() - before;
+        g_launches.fetch_sub(kernels);  // captured, not launched
+        const cudaError_t e = cudaStreamEndCapture(s, &gr);
+        if (!ok || e != cudaSuccess || !gr || cudaGraphInstantiate(&exec, gr, 0) != cudaSuccess) {
+            exec = nullptr;
+            failed = true;
+        }
+        if (gr) cudaGraphDestroy(gr);
+        cudaGetLastError();
+    }
+};
+
 struct LoopState {
     int iterations = 0;
     int sum_class = 0;
@@ -113,17 +179,49 @@ static LoopState run_loop(tc_ctx* ctx, const tc_job* job, const float* x, int k,
     st.iterations = cap;
     double old_inertia = 1e10;
     int countIter = 0;
+    // what the stages leave in aux: changed (+0), dist sum (+8), sum_class and the
+    // bad-label flag (+16), error words of the Gram and the correlation (+48)
     struct {
         int32_t changed;
         int32_t pad;
         double dsum;
+        int32_t sum_class, bad_label;
+        int32_t pad2[6];
+        int32_t err[2];
     } h;
-    auto do_assign = [&]() -> bool {
-        TC_CUDA(cudaMemsetAsync(aux, 0, 16, s));
-        // no shifts here: an extraction whose gate opens computes them itself
-        assign(ctx, x, C, n, m, k, job->mode, job->precision, labels, dist, nullptr, old, changed, dsum, s);
-        TC_CUDA(cudaMemcpyAsync(&h, aux, 16, cudaMemcpyDeviceToHost, s));
+    static_assert(sizeof(h) == 56, "aux layout");
+    StageGraph g_extract, g_assign;
+    const bool graphs = !std::getenv("TIMESC_NO_GRAPHS");
+    auto readback = [&]() {
+        TC_CUDA(cudaMemcpyAsync(&h, aux, sizeof(h), cudaMemcpyDeviceToHost, s));
         TC_CUDA(cudaStreamSynchronize(s));
+        check_async_errors(h.err);
+    };
+    TC_CUDA(cudaMemsetAsync(aux, 0, 64, s));
+    auto issue_assign = [&]() {
+        TC_CUDA(cudaMemsetAsync(aux, 0, 16, s));
+        // no shifts here: the extraction computes its own where the gate is open
+        assign(ctx, x, C, n, m, k, job->mode, job->precision, labels, dist, nullptr, old, changed, dsum, s);
+    };
+    ExtractArgs e{};
+    e.x = x;
+    e.labels = labels;
+    e.shift = nullptr;
+    e.C = C;
+    e.n = n;
+    e.m = m;
+    e.k = k;
+    e.mode = job->mode;
+    e.cal_select = cal_select;
+    e.precision = job->precision;
+    e.counts = nullptr;
+    auto issue_extract = [&]() {
+        extract_async(ctx, e, s);
+        TC_CUDA(cudaMemcpyAsync(aux + 16, ws.scal.p, 2 * sizeof(int32_t), cudaMemcpyDeviceToDevice, s));
+    };
+    auto do_assign = [&]() -> bool {
+        g_assign.run(graphs, s, issue_assign);
+        readback();
         st.inertia = h.dsum / (double)n;
         return h.changed == 0;
     };
@@ -142,20 +240,10 @@ static LoopState run_loop(tc_ctx* ctx, const tc_job* job, const float* x, int k,
         return false;
     };
     auto extract = [&]() {
-        ExtractArgs e{};
-        e.x = x;
-        e.labels = labels;
-        e.shift = nullptr;
-        e.C = C;
-        e.n = n;
-        e.m = m;
-        e.k = k;
-        e.mode = job->mode;
-        e.cal_select = cal_select;
-        e.precision = job->precision;
-        e.counts = nullptr;
-        int sc = run_extract(ctx, e, s);
-        if (!cal_select) st.sum_class = sc;  // get_class_centers_a leaves sum_class alone
+        g_extract.run(graphs, s, issue_extract);
+        readback();
+        TC_REQUIRE(h.bad_label == 0, TC_ERR_ARG, "a label is outside [0, k)");
+        if (!cal_select) st.sum_class = h.sum_class;  // get_class_centers_a leaves sum_class alone
     };
     for (int i = 0; i < cap; ++i) {
         if (!order_tsl) {
@@ -284,8 +372,17 @@ int tc_sbd_assign(tc_ctx* ctx, const float* d_x, const float* d_centroids, int64
     TC_REQUIRE((d_x && d_centroids && d_labels) || n == 0, TC_ERR_ARG, "null pointer");
     TC_REQUIRE(precision >= TC_PREC_FP32 && precision <= TC_PREC_TF32, TC_ERR_ARG, "unknown precision");
     TC_CUDA(cudaSetDevice(ctx->device));
+    cudaStream_t s = (cudaStream_t)stream;
+    int* words = reinterpret_cast<int*>(ctx->ws.aux.as<char>(64) + 48);
+    TC_CUDA(cudaMemsetAsync(words, 0, 2 * sizeof(int), s));
     assign(ctx, d_x, d_centroids, n, m, k, mode, precision, d_labels, d_dist, d_shift, d_old_labels, d_changed,
-           d_dist_sum, (cudaStream_t)stream);
+           d_dist_sum, s);
+    if (precision != TC_PREC_FP32) {  // the tensor-core path reports through an error word
+        int h[2] = {0, 0};
+        TC_CUDA(cudaMemcpyAsync(h, words, sizeof(h), cudaMemcpyDeviceToHost, s));
+        TC_CUDA(cudaStreamSynchronize(s));
+        check_async_errors(h);
+    }
     TC_API_END(ctx)
 }
 

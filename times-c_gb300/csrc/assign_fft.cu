@@ -200,6 +200,7 @@ struct AssignParams {
     int64_t n;
     int m, k, F, clamp2;
     const int32_t* fixed;
+    const uint8_t* gate;  // with fixed: series whose centroid's gate is closed get shift 0, no work
     int32_t* labels;
     float* dist;
     int32_t* shift;
@@ -258,6 +259,10 @@ __global__ void __launch_bounds__(Cfg<N>::BLOCK, 1) k_assign_fft(AssignParams p)
     int nchg = 0;
     const int64_t stride = (int64_t)gridDim.x * TEAMS;
     for (int64_t i = (int64_t)blockIdx.x * TEAMS + team; i < p.n; i += stride) {
+        if (p.fixed && p.gate && !p.gate[p.fixed[i]]) {  // uniform over the team
+            if (tid == 0 && p.shift) p.shift[i] = 0;
+            continue;
+        }
         float2 xh[2][Co::R0];
         float xhN = 0.f;
         double nrm2;
@@ -357,6 +362,7 @@ static void assign_n(tc_ctx* ctx, const AssignArgs& a, cudaStream_t s) {
     p.F = a.F;
     p.clamp2 = a.clamp2;
     p.fixed = a.fixed;
+    p.gate = a.gate;
     p.labels = a.labels;
     p.dist = a.dist;
     p.shift = a.shift;

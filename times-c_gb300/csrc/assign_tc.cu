@@ -411,10 +411,8 @@ void launch_assign_tc(tc_ctx* ctx, const AssignArgs& a, int precision, cudaStrea
     const int grid = (int)std::min<int64_t>(ntiles, ctx->sm_count);
     k_assign_tc<<<grid, AT_THREADS, smem, s>>>(map, p);
     TC_CHECK_LAUNCH();
-    int h_err = 0;
-    TC_CUDA(cudaMemcpyAsync(&h_err, err, sizeof(int), cudaMemcpyDeviceToHost, s));
-    TC_CUDA(cudaStreamSynchronize(s));
-    TC_REQUIRE(h_err == 0, TC_ERR_TIMEOUT, "tensor-core correlation: a pipeline wait ran out");
+    // no synchronisation here: a pipeline wait that ran out leaves the error word at
+    // aux+52 set, and the caller reads it with its other results
 }
 
 }  // namespace tc

@@ -26,8 +26,9 @@ void launch_gather_norm(const float* x, const int32_t* perm, const int32_t* labe
                         const uint8_t* gate, int64_t n, int m, float* seg, int sm_count, cudaStream_t s);
 bool gram_tc_supported(int m, int precision);
 void launch_gram_tc(tc_ctx* ctx, const float* seg, const int32_t* counts, const int32_t* offsets,
-                    const std::vector<int32_t>& h_counts, int64_t n, int k, int m, int ld, int precision,
-                    float* S, cudaStream_t s);
+                    const int64_t* poff, int64_t n, int k, int m, int ld, int precision, float* S, int* err,
+                    cudaStream_t s);
+int64_t gram_padded_cols(int64_t n, int k);
 
 constexpr int SEG_CHUNK = 4096;
 constexpr int SEG_BLOCK = 256;
@@ -103,13 +104,18 @@ __global__ void k_seg_scan_chunks(int32_t* __restrict__ chunk_cnt, int nchunks, 
     if (threadIdx.x == 0) counts[j] = carry;
 }
 
+// offsets, sum_class and (for the tensor-core Gram) offsets of the clusters
+// padded to multiples of 64 members.
 __global__ void k_seg_offsets(const int32_t* __restrict__ counts, int k, int32_t* __restrict__ offsets,
-                              int32_t* __restrict__ sum_class) {
+                              int32_t* __restrict__ sum_class, int64_t* __restrict__ poff) {
     if (threadIdx.x == 0) {
         int acc = 0, nz = 0;
+        int64_t pacc = 0;
         for (int j = 0; j < k; ++j) {
             offsets[j] = acc;
+            if (poff) poff[j] = pacc;
             acc += counts[j];
+            pacc += (counts[j] + 63) / 64 * 64;
             nz += counts[j] != 0;
         }
         *sum_class = nz;
@@ -265,7 +271,11 @@ void power_eigvecs(tc_ctx* ctx, const float* S, int ld, const double* r, const d
                    cudaStream_t s);
 
 // ---------------------------------------------------------------- driver
-int run_extract(tc_ctx* ctx, const ExtractArgs& a, cudaStream_t s) {
+// Everything on the stream, with no host synchronisation (capturable in a CUDA
+// graph): the alignment shifts are computed for every series whose centroid's
+// gate is open (the kernel skips the others), and the flags stay on the device:
+// scal[0] = sum_class, scal[1] = a label outside [0, k), Gram error word at aux+48.
+void extract_async(tc_ctx* ctx, const ExtractArgs& a, cudaStream_t s) {
     Workspace& ws = ctx->ws;
     const int64_t n = a.n;
     const int m = a.m, k = a.k;
@@ -276,6 +286,7 @@ int run_extract(tc_ctx* ctx, const ExtractArgs& a, cudaStream_t s) {
     int32_t* chunk = ws.chunk_counts.as<int32_t>((size_t)std::max(nchunks, 1) * k);
     int32_t* counts = a.counts ? a.counts : ws.counts.as<int32_t>(k);
     int32_t* offsets = ws.offsets.as<int32_t>(k);
+    int64_t* poff = ws.gram_poff.as<int64_t>(k);
     uint8_t* gate = ws.gate.as<uint8_t>(k);
     int32_t* scal = ws.scal.as<int32_t>(16);
     float* seg = ws.seg.as<float>((size_t)std::max<int64_t>(n, 1) * m);
@@ -283,6 +294,7 @@ int run_extract(tc_ctx* ctx, const ExtractArgs& a, cudaStream_t s) {
     float* S = ws.gram.as<float>((size_t)k * m * ld);
     double* rs = ws.rowsum.as<double>((size_t)k * m + k);
     double* tot = rs + (size_t)k * m;
+    int* gram_err = reinterpret_cast<int*>(ws.aux.as<char>(64) + 48);
 
     TC_CUDA(cudaMemsetAsync(scal, 0, sizeof(int32_t) * 16, s));
     if (n > 0) {
@@ -293,7 +305,7 @@ int run_extract(tc_ctx* ctx, const ExtractArgs& a, cudaStream_t s) {
     }
     k_seg_scan_chunks<<<k, 256, 0, s>>>(chunk, std::max(nchunks, 1), k, counts);
     TC_CHECK_LAUNCH();
-    k_seg_offsets<<<1, 32, 0, s>>>(counts, k, offsets, scal);
+    k_seg_offsets<<<1, 32, 0, s>>>(counts, k, offsets, scal, poff);
     TC_CHECK_LAUNCH();
     if (n > 0) {
         size_t smem = (size_t)9 * k * sizeof(int);
@@ -304,20 +316,8 @@ int run_extract(tc_ctx* ctx, const ExtractArgs& a, cudaStream_t s) {
     k_gate<<<k, 256, 0, s>>>(a.C, m, a.mode, gate);
     TC_CHECK_LAUNCH();
 
-    // one small read-back: counts, gates, sum_class
-    std::vector<int32_t> h_counts(k);
-    std::vector<uint8_t> h_gate(k);
-    int32_t h_sc[2] = {0, 0};
-    TC_CUDA(cudaMemcpyAsync(h_counts.data(), counts, sizeof(int32_t) * k, cudaMemcpyDeviceToHost, s));
-    TC_CUDA(cudaMemcpyAsync(h_gate.data(), gate, k, cudaMemcpyDeviceToHost, s));
-    TC_CUDA(cudaMemcpyAsync(h_sc, scal, sizeof(int32_t) * 2, cudaMemcpyDeviceToHost, s));
-    TC_CUDA(cudaStreamSynchronize(s));
-    TC_REQUIRE(h_sc[1] == 0, TC_ERR_ARG, "a label is outside [0, k)");
-    bool any_gate = false;
-    for (int j = 0; j < k; ++j) any_gate |= (h_gate[j] && h_counts[j] > 0);
-
     const int32_t* shift = a.shift;
-    if (any_gate && !shift) {
+    if (!shift && n > 0) {
         // alignment shifts of each series against its own centroid (sbd3D, SBD.cuh:69-85)
         const int F = fft_size(m, a.mode);
         float2* spec = ws.spectra.as<float2>((size_t)k * (F / 2 + 1));
@@ -332,18 +332,19 @@ int run_extract(tc_ctx* ctx, const ExtractArgs& a, cudaStream_t s) {
         aa.F = F;
         aa.clamp2 = 0;
         aa.fixed = a.labels;
+        aa.gate = gate;
         aa.shift = sh;
         launch_assign_fft(ctx, aa, s);
         shift = sh;
     }
-    launch_gather_norm(a.x, perm, a.labels, any_gate ? shift : nullptr, any_gate ? gate : nullptr, n, m, seg,
-                       ctx->sm_count, s);
+    launch_gather_norm(a.x, perm, a.labels, shift, gate, n, m, seg, ctx->sm_count, s);
 
     // Gram (padding columns b in [m, ld) stay zero)
     if (ld != m) TC_CUDA(cudaMemsetAsync(S, 0, sizeof(float) * (size_t)k * m * ld, s));
+    TC_CUDA(cudaMemsetAsync(gram_err, 0, sizeof(int), s));
     const int nt = ceil_div(m, 64);
     if (gram_tc_supported(m, a.precision)) {
-        launch_gram_tc(ctx, seg, counts, offsets, h_counts, n, k, m, ld, a.precision, S, s);
+        launch_gram_tc(ctx, seg, counts, offsets, poff, n, k, m, ld, a.precision, S, gram_err, s);
     } else {
         dim3 g(nt * (nt + 1) / 2, k);
         k_gram_simt<<<g, 256, 0, s>>>(seg, counts, offsets, m, ld, nt, S);
@@ -360,6 +361,17 @@ int run_extract(tc_ctx* ctx, const ExtractArgs& a, cudaStream_t s) {
     const int tmax = full ? std::max(4 * m, 200) : m;
     const double tol = full ? 5e-7 : 1e-6;
     power_eigvecs(ctx, S, ld, rs, tot, counts, offsets, seg, k, m, a.mode, tmax, tol, a.C, s);
+}
+
+int run_extract(tc_ctx* ctx, const ExtractArgs& a, cudaStream_t s) {
+    extract_async(ctx, a, s);
+    int32_t h_sc[2] = {0, 0};
+    int h_err = 0;
+    TC_CUDA(cudaMemcpyAsync(h_sc, ctx->ws.scal.p, sizeof(int32_t) * 2, cudaMemcpyDeviceToHost, s));
+    TC_CUDA(cudaMemcpyAsync(&h_err, static_cast<char*>(ctx->ws.aux.p) + 48, sizeof(int), cudaMemcpyDeviceToHost, s));
+    TC_CUDA(cudaStreamSynchronize(s));
+    TC_REQUIRE(h_sc[1] == 0, TC_ERR_ARG, "a label is outside [0, k)");
+    TC_REQUIRE(h_err == 0, TC_ERR_TIMEOUT, "tensor-core Gram: a pipeline wait ran out");
     return h_sc[0];
 }
 

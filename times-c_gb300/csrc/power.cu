@@ -368,7 +368,9 @@ void power_eigvecs(tc_ctx* ctx, const float* S, int ld, const double* r, const d
         else if (nv4 <= 128) launch_cluster<8, 4>(pp, k, smem, s);
         else launch_cluster<8, 8>(pp, k, smem, s);
     }
-    if (std::getenv("TIMESC_TRACE")) {
+    cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+    TC_CUDA(cudaStreamIsCapturing(s, &cap));
+    if (std::getenv("TIMESC_TRACE") && cap == cudaStreamCaptureStatusNone) {
         std::vector<int> h(k);
         TC_CUDA(cudaMemcpyAsync(h.data(), steps, sizeof(int) * k, cudaMemcpyDeviceToHost, s));
         TC_CUDA(cudaStreamSynchronize(s));

@@ -126,6 +126,7 @@ struct AssignArgs {
     int m, k, F;
     int clamp2;                // pad value 2 of get_pos_idx (compat, 2m-1 < 512)
     const int32_t* fixed;      // if set: evaluate only centroid fixed[i] (alignment shifts)
+    const uint8_t* gate;       // with fixed: skip series whose centroid's gate is closed (shift 0)
     int32_t* labels;
     float* dist;
     int32_t* shift;
@@ -151,7 +152,10 @@ struct ExtractArgs {
     int m, k, mode, cal_select, precision;
     int32_t* counts;           // k
 };
-// returns sum_class (synchronises)
+// no host synchronisation: sum_class and the bad-label flag stay in ws.scal[0..1],
+// the Gram error word at aux+48
+void extract_async(tc_ctx* ctx, const ExtractArgs& a, cudaStream_t s);
+// extract_async, then reads and checks the flags; returns sum_class
 int run_extract(tc_ctx* ctx, const ExtractArgs& a, cudaStream_t s);
 
 // helpers

@@ -247,25 +247,45 @@ bool gram_tc_supported(int m, int precision) {
     return m >= 2;
 }
 
-void launch_gram_tc(tc_ctx* ctx, const float* seg, const int32_t* counts, const int32_t* offsets,
-                    const std::vector<int32_t>& h_counts, int64_t n, int k, int m, int ld, int precision,
-                    float* S, cudaStream_t s) {
-    Workspace& ws = ctx->ws;
-    std::vector<int64_t> hp(k);
-    int64_t Pp = 0;
-    for (int j = 0; j < k; ++j) {
-        hp[j] = Pp;
-        Pp += (h_counts[j] + GT_PAD - 1) / GT_PAD * GT_PAD;
+// Zero the padding columns of cluster c: [poff + count, poff + roundup(count, 64)), every row.
+template <class TO>
+__global__ void k_zero_pads(const int32_t* __restrict__ counts, const int64_t* __restrict__ poff, int m, int64_t Pp,
+                            TO* __restrict__ YT, float* __restrict__ YTlo) {
+    const int c = blockIdx.x;
+    const int cnt = counts[c];
+    const int pad = (cnt + GT_PAD - 1) / GT_PAD * GT_PAD - cnt;
+    const int64_t c0 = poff[c] + cnt;
+    for (int e = threadIdx.x; e < pad * m; e += blockDim.x) {
+        const int a = e / pad, q = e % pad;
+        YT[(int64_t)a * Pp + c0 + q] = TO(0.f);
+        if (YTlo) YTlo[(int64_t)a * Pp + c0 + q] = 0.f;
     }
-    Pp = std::max<int64_t>(Pp, GT_PAD);
-    int64_t* poff = ws.gram_poff.as<int64_t>(k);
-    TC_CUDA(cudaMemcpyAsync(poff, hp.data(), sizeof(int64_t) * k, cudaMemcpyHostToDevice, s));
+}
+
+// Columns of the transposed, cluster-padded member matrix: every cluster padded
+// to a multiple of 64 members fits in n + 63 k (the padded offsets themselves
+// are computed on the device, so the layout needs no host read-back).
+int64_t gram_padded_cols(int64_t n, int k) {
+    return std::max<int64_t>((n + 63 * (int64_t)k + GT_PAD - 1) / GT_PAD * GT_PAD, GT_PAD);
+}
+
+// No host synchronisation: a pipeline wait that runs out sets *err (the caller reads it).
+void launch_gram_tc(tc_ctx* ctx, const float* seg, const int32_t* counts, const int32_t* offsets,
+                    const int64_t* poff, int64_t n, int k, int m, int ld, int precision, float* S, int* err,
+                    cudaStream_t s) {
+    Workspace& ws = ctx->ws;
+    const int64_t Pp = gram_padded_cols(n, k);
     const int fmt = precision == TC_PREC_BF16 ? 1 : (precision == TC_PREC_TF32 ? 2 : 3);
     const int esize = fmt == 1 ? 2 : 4;
     const size_t plane = (size_t)m * Pp * esize;
     char* YT = static_cast<char*>(ws.gram_yt.get(plane * (fmt == 3 ? 2 : 1)));
     float* YTlo = fmt == 3 ? reinterpret_cast<float*>(YT + plane) : nullptr;
-    TC_CUDA(cudaMemsetAsync(YT, 0, plane * (fmt == 3 ? 2 : 1), s));
+    // only the padding needs zeros: the transpose writes every member column
+    if (fmt == 1)
+        k_zero_pads<__nv_bfloat16><<<k, 256, 0, s>>>(counts, poff, m, Pp, (__nv_bfloat16*)YT, nullptr);
+    else
+        k_zero_pads<float><<<k, 256, 0, s>>>(counts, poff, m, Pp, (float*)YT, YTlo);
+    TC_CHECK_LAUNCH();
     dim3 tg(ceil_div(n, 32), ceil_div(m, 32)), tb(32, 8);
     if (n > 0) {
         if (fmt == 1)
@@ -278,8 +298,6 @@ void launch_gram_tc(tc_ctx* ctx, const float* seg, const int32_t* counts, const 
     const CUtensorMapDataType dt = fmt == 1 ? CU_TENSOR_MAP_DATA_TYPE_BFLOAT16 : CU_TENSOR_MAP_DATA_TYPE_FLOAT32;
     CUtensorMap map = make_tmap_2d(YT, dt, esize, (uint64_t)m, (uint64_t)Pp, GT_TILE);
     CUtensorMap map_lo = fmt == 3 ? make_tmap_2d(YTlo, dt, esize, (uint64_t)m, (uint64_t)Pp, GT_TILE) : map;
-    int* err = reinterpret_cast<int*>(ws.aux.as<char>(64) + 48);
-    TC_CUDA(cudaMemsetAsync(err, 0, sizeof(int), s));
     const int nt = ceil_div(m, GT_TILE);
     dim3 grid(nt * (nt + 1) / 2, k);
     if (fmt == 1) {
@@ -293,10 +311,6 @@ void launch_gram_tc(tc_ctx* ctx, const float* seg, const int32_t* counts, const 
         k_gram_tc<3><<<grid, 128, GtCfg<3>::SMEM, s>>>(map, map_lo, counts, poff, m, ld, nt, S, err);
     }
     TC_CHECK_LAUNCH();
-    int h_err = 0;
-    TC_CUDA(cudaMemcpyAsync(&h_err, err, sizeof(int), cudaMemcpyDeviceToHost, s));
-    TC_CUDA(cudaStreamSynchronize(s));
-    TC_REQUIRE(h_err == 0, TC_ERR_TIMEOUT, "tensor-core Gram: a pipeline wait ran out");
 }
 
 }  // namespace tc
