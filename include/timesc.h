@@ -165,6 +165,45 @@ typedef struct {
  * init_chose), apply the restart rule, copy labels/centroids out.  Synchronous. */
 int tc_kshape_run(tc_ctx* ctx, const tc_job* job, tc_result* result);
 
+/* ---------------------------------------------------------------- many jobs: batch and serving */
+/* No counterpart in the reference, which runs one job per process.  A pool owns
+ * `workers` contexts (each a stream and a workspace) and host threads that run
+ * tc_kshape_run on them, so the iterations of different jobs overlap on the
+ * device.  Admission: the device memory held by the workers' workspaces, plus
+ * the footprint (tc_job_footprint) reserved for each running job, stays within
+ * hbm_budget_bytes; a job starts when a worker is free and its footprint fits,
+ * idle workers give their workspaces back when a job needs the room, and a job
+ * larger than the budget is rejected (TC_ERR_REJECTED). */
+typedef struct {
+    int workers;                  /* jobs in flight at once; <= 0 means 8 */
+    uint64_t hbm_budget_bytes;    /* 0 means 80% of the device memory free at creation */
+} tc_pool_opts;
+
+typedef struct tc_pool tc_pool;
+
+int tc_pool_create(int device, const tc_pool_opts* opts, tc_pool** out);
+/* Waits for every submitted job, then frees the workers. */
+int tc_pool_destroy(tc_pool* pool);
+/* Upper estimate of the device bytes a worker's workspace grows by for job. */
+uint64_t tc_job_footprint(const tc_job* job);
+
+/* Batch: runs jobs[0..njobs) to completion, largest estimated work first;
+ * statuses[i] (if not NULL) gets job i's tc_status.  Returns TC_OK, or the first
+ * failing status.  The job's host buffers and result stay the caller's. */
+int tc_pool_run_batch(tc_pool* pool, const tc_job* jobs, int njobs, tc_result* results, int* statuses);
+
+/* Serving: queue one job (FIFO; a job that does not fit the memory left lets
+ * smaller queued jobs start first).  *job and *result must stay valid until the
+ * job is waited for.  Returns TC_ERR_REJECTED at once for a job larger than the
+ * budget. */
+int tc_pool_submit(tc_pool* pool, const tc_job* job, tc_result* result, uint64_t* ticket);
+/* Blocks until the job is done; *status = its tc_status, *queued_s = seconds from
+ * submission to start, *latency_s = seconds from submission to completion (any
+ * output pointer may be NULL). */
+int tc_pool_wait(tc_pool* pool, uint64_t ticket, int* status, double* queued_s, double* latency_s);
+/* Jobs running and queued now, and the bytes held or reserved by the workers. */
+int tc_pool_stats(tc_pool* pool, int* running, int* queued, uint64_t* held_bytes);
+
 /* ---------------------------------------------------------------- host I/O */
 /* Parse a text file: one series per line, values separated by commas (a line
  * with a comma is split on commas only) or else by spaces/tabs.  labeled=1: the

@@ -1,4 +1,5 @@
 """Host-side product code and the C ABI surface (CPU only, no GPU calls)."""
+import ctypes
 import os
 import re
 import subprocess
@@ -142,3 +143,24 @@ def test_cli_argument_handling():
     assert subprocess.run([cli, "-d", "0", "x"], capture_output=True).returncode == 2
     assert subprocess.run([cli, "-d", "0", "f", "4", "1", "0", "--mode", "bogus"],
                           capture_output=True).returncode == 2
+
+
+def test_job_footprint_estimate(built):
+    """tc_job_footprint (pool admission) is a host computation: it grows with n, m
+    and k, counts the BF16 series copy of the tensor-core path, and is 0 for an
+    invalid job."""
+    T, _ = built
+    lib = T.lib()
+
+    def fp(n, m, k, prec=0, mode=0):
+        j = T.Job(None, None, n, m, k, mode, prec, 0, 0, 10, 1, None)
+        return int(lib.tc_job_footprint(ctypes.byref(j)))
+
+    base = fp(10000, 512, 8)
+    assert base > 2 * 10000 * 512 * 4
+    assert fp(20000, 512, 8) > base and fp(10000, 1024, 8) > base and fp(10000, 512, 16) > base
+    # BF16 at m <= 512: the BF16 series copy (n*512*2) on top of the FP32 buffers and BF16 Gram planes
+    assert fp(10000, 512, 8, prec=1) >= 2 * 10000 * 512 * 4 + 2 * 10000 * 512 * 2
+    assert fp(0, 512, 8) == 0 and fp(100, 1, 8) == 0
+    # the serving form's large request (n=2e5, m=1024, k=16) stays in the single-digit GB
+    assert 2e9 < fp(200000, 1024, 16) < 1e10

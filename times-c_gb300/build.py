@@ -21,11 +21,11 @@ CLI = os.path.join(BIN_DIR, "test")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr",
               "-I", os.path.join(ROOT, "include"), "-I", CSRC] + ARCH
-CXX_FLAGS = ["-O2", "-std=c++17", "-fPIC", "-I", os.path.join(ROOT, "include"), "-I", CSRC,
+CXX_FLAGS = ["-O2", "-std=c++17", "-fPIC", "-pthread", "-I", os.path.join(ROOT, "include"), "-I", CSRC,
              "-I", "/usr/local/cuda/include"]
 
 CU_SOURCES = ["assign_fft.cu", "znorm.cu", "extract.cu", "power.cu", "tensor_core.cu", "assign_tc.cu"]
-CPP_SOURCES = ["api.cpp", "io.cpp", "gen.cpp"]
+CPP_SOURCES = ["api.cpp", "io.cpp", "gen.cpp", "pool.cpp"]
 
 
 def _run(cmd):

@@ -265,6 +265,25 @@ static LoopState run_loop(tc_ctx* ctx, const tc_job* job, const float* x, int k,
     return st;
 }
 
+static std::vector<DevBuf*> workspace_buffers(tc_ctx* ctx) {
+    Workspace& w = ctx->ws;
+    return {&w.x,    &w.labels,  &w.old_labels, &w.shift,   &w.dist,      &w.centroids, &w.spectra,
+            &w.seg,  &w.perm,    &w.chunk_counts, &w.counts, &w.offsets,  &w.gate,      &w.scal,
+            &w.gram, &w.rowsum,  &w.gram_yt,    &w.gram_poff, &w.piter,   &w.pstats,    &w.aux,
+            &w.toeplitz, &w.toeplitz_norm, &w.xbf, &w.xbf_norm};
+}
+
+void release_workspace(tc_ctx* ctx) {
+    for (DevBuf* b : workspace_buffers(ctx)) b->release();
+    ctx->prep_x = nullptr;
+}
+
+size_t workspace_bytes(tc_ctx* ctx) {
+    size_t t = 0;
+    for (DevBuf* b : workspace_buffers(ctx)) t += b->bytes;
+    return t;
+}
+
 }  // namespace tc
 
 using namespace tc;
@@ -318,12 +337,7 @@ int tc_destroy(tc_ctx* ctx) {
     if (!ctx) return TC_ERR_ARG;
     cudaSetDevice(ctx->device);
     cudaStreamSynchronize(ctx->own_stream);
-    DevBuf* bufs[] = {&ctx->ws.x, &ctx->ws.labels, &ctx->ws.old_labels, &ctx->ws.shift, &ctx->ws.dist,
-                      &ctx->ws.centroids, &ctx->ws.spectra, &ctx->ws.seg, &ctx->ws.perm, &ctx->ws.chunk_counts,
-                      &ctx->ws.counts, &ctx->ws.offsets, &ctx->ws.gate, &ctx->ws.scal, &ctx->ws.gram,
-                      &ctx->ws.rowsum, &ctx->ws.gram_yt, &ctx->ws.gram_poff, &ctx->ws.piter, &ctx->ws.pstats, &ctx->ws.aux, &ctx->ws.toeplitz,
-                      &ctx->ws.toeplitz_norm, &ctx->ws.xbf, &ctx->ws.xbf_norm};
-    for (DevBuf* b : bufs) b->release();
+    tc::release_workspace(ctx);
     for (auto* t : ctx->fft) {
         t->twN.release();
         t->twF.release();

@@ -260,10 +260,23 @@ __global__ void k_rowsum(const float* __restrict__ S, const int32_t* __restrict_
     double d = s;
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) d += __shfl_xor_sync(0xffffffffu, d, o);
-    if (lane == 0) {
-        r[(size_t)c * m + a] = d;
-        atomicAdd(&tot[c], d);
+    if (lane == 0) r[(size_t)c * m + a] = d;
+}
+
+// tot[c] = sum_a r[c][a] in a fixed order (no atomics: the result, and the
+// power iteration that uses it, is the same on every run)
+__global__ void k_rowsum_total(const double* __restrict__ r, const int32_t* __restrict__ counts, int m,
+                               double* __restrict__ tot) {
+    __shared__ double red[32];
+    const int c = blockIdx.x;
+    if (counts[c] == 0) {
+        if (threadIdx.x == 0) tot[c] = 0.0;
+        return;
     }
+    double s = 0.0;
+    for (int a = threadIdx.x; a < m; a += blockDim.x) s += r[(size_t)c * m + a];
+    s = block_sum_d(s, red);
+    if (threadIdx.x == 0) tot[c] = s;
 }
 
 void power_eigvecs(tc_ctx* ctx, const float* S, int ld, const double* r, const double* tot, const int32_t* counts,
@@ -350,8 +363,9 @@ void extract_async(tc_ctx* ctx, const ExtractArgs& a, cudaStream_t s) {
         k_gram_simt<<<g, 256, 0, s>>>(seg, counts, offsets, m, ld, nt, S);
         TC_CHECK_LAUNCH();
     }
-    TC_CUDA(cudaMemsetAsync(tot, 0, sizeof(double) * k, s));
     k_rowsum<<<dim3(ceil_div(m, 8), k), 256, 0, s>>>(S, counts, m, ld, rs, tot);
+    TC_CHECK_LAUNCH();
+    k_rowsum_total<<<k, 256, 0, s>>>(rs, counts, m, tot);
     TC_CHECK_LAUNCH();
 
     // power iteration: compat runs at most m steps (the reference's fixed count),

@@ -158,6 +158,10 @@ void extract_async(tc_ctx* ctx, const ExtractArgs& a, cudaStream_t s);
 // extract_async, then reads and checks the flags; returns sum_class
 int run_extract(tc_ctx* ctx, const ExtractArgs& a, cudaStream_t s);
 
+// workspace of a context: free every buffer (the context must be idle) / bytes held
+void release_workspace(tc_ctx* ctx);
+size_t workspace_bytes(tc_ctx* ctx);
+
 // helpers
 inline int ceil_div(int64_t a, int64_t b) { return (int)((a + b - 1) / b); }
 int fft_size(int m, int mode);

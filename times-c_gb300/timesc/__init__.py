@@ -41,6 +41,10 @@ class Result(ctypes.Structure):
                 ("restarted", _int), ("inertia", ctypes.c_double), ("seconds", ctypes.c_double)]
 
 
+class PoolOpts(ctypes.Structure):
+    _fields_ = [("workers", _int), ("hbm_budget_bytes", ctypes.c_uint64)]
+
+
 class GenSpec(ctypes.Structure):
     _fields_ = [("n", _i64), ("m", _int), ("classes", _int), ("noise", ctypes.c_double),
                 ("dirichlet", ctypes.c_double), ("seed", ctypes.c_uint64)]
@@ -62,6 +66,14 @@ SIGNATURES = {
     "tc_extract_shapes": (_int, [_vp, _vp, _vp, _vp, _vp, _i64, _int, _int, _int, _int, _int, _vp,
                                  ctypes.POINTER(_int), _vp]),
     "tc_kshape_run": (_int, [_vp, ctypes.POINTER(Job), ctypes.POINTER(Result)]),
+    "tc_pool_create": (_int, [_int, ctypes.POINTER(PoolOpts), ctypes.POINTER(_vp)]),
+    "tc_pool_destroy": (_int, [_vp]),
+    "tc_job_footprint": (ctypes.c_uint64, [ctypes.POINTER(Job)]),
+    "tc_pool_run_batch": (_int, [_vp, _vp, _int, _vp, _vp]),
+    "tc_pool_submit": (_int, [_vp, ctypes.POINTER(Job), ctypes.POINTER(Result), ctypes.POINTER(ctypes.c_uint64)]),
+    "tc_pool_wait": (_int, [_vp, ctypes.c_uint64, ctypes.POINTER(_int), ctypes.POINTER(ctypes.c_double),
+                            ctypes.POINTER(ctypes.c_double)]),
+    "tc_pool_stats": (_int, [_vp, ctypes.POINTER(_int), ctypes.POINTER(_int), ctypes.POINTER(ctypes.c_uint64)]),
     "tc_read_file": (_int, [ctypes.c_char_p, _int, ctypes.POINTER(_fp), ctypes.POINTER(_i32p),
                             ctypes.POINTER(_i64), ctypes.POINTER(_int), ctypes.c_char_p, _int]),
     "tc_free_host": (None, [_vp]),
@@ -185,6 +197,86 @@ class Context:
         self._check(lib().tc_kshape_run(self.h, ctypes.byref(job), ctypes.byref(res)))
         return dict(labels=labels, centroids=cents, iterations=res.iterations, sum_class=res.sum_class,
                     restarted=res.restarted, inertia=res.inertia, seconds=res.seconds)
+
+
+class JobSpec:
+    """One job for a Pool: host data (n x m float32) and the tc_kshape_run options.
+    Keeps the arrays the C side points at alive until the job is collected."""
+
+    def __init__(self, data, k, mode=MODE_COMPAT, precision=PREC_FP32, init_chose=0, seed=0, max_iter=20,
+                 restart=True, init_labels=None):
+        self.data = np.ascontiguousarray(data, dtype=np.float32)
+        n, m = self.data.shape
+        self.k = k
+        self.labels = np.zeros(n, np.int32)
+        self.centroids = np.zeros((k, m), np.float32)
+        self.init = None if init_labels is None else np.ascontiguousarray(init_labels, dtype=np.int32)
+        self.job = Job(self.data.ctypes.data, None, n, m, k, mode, precision, init_chose, seed, max_iter,
+                       int(restart), None if self.init is None else self.init.ctypes.data)
+        self.res = Result(self.labels.ctypes.data, self.centroids.ctypes.data, 0, 0, 0, 0.0, 0.0)
+
+    def footprint(self):
+        return int(lib().tc_job_footprint(ctypes.byref(self.job)))
+
+    def result(self):
+        r = self.res
+        return dict(labels=self.labels, centroids=self.centroids, iterations=r.iterations, sum_class=r.sum_class,
+                    restarted=r.restarted, inertia=r.inertia, seconds=r.seconds)
+
+
+class Pool:
+    """Workers (contexts + host threads) running many jobs concurrently on one GPU:
+    run_batch for a fixed set, submit/wait for continuous serving."""
+
+    def __init__(self, device=0, workers=8, hbm_budget_bytes=0):
+        h = _vp()
+        opts = PoolOpts(workers, hbm_budget_bytes)
+        rc = lib().tc_pool_create(device, ctypes.byref(opts), ctypes.byref(h))
+        if rc != OK:
+            raise TimescError(rc, "tc_pool_create failed")
+        self.h = h
+        self._live = {}
+
+    def close(self):
+        if self.h:
+            lib().tc_pool_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        self.close()
+
+    def run_batch(self, specs):
+        """Runs JobSpecs to completion; returns their tc_status codes."""
+        n = len(specs)
+        jobs = (Job * n)(*[s.job for s in specs])
+        results = (Result * n)(*[s.res for s in specs])
+        st = (_int * n)()
+        lib().tc_pool_run_batch(self.h, jobs, n, results, st)
+        for i, s in enumerate(specs):
+            s.res = results[i]
+        return list(st)
+
+    def submit(self, spec):
+        t = ctypes.c_uint64()
+        rc = lib().tc_pool_submit(self.h, ctypes.byref(spec.job), ctypes.byref(spec.res), ctypes.byref(t))
+        if rc != OK:
+            raise TimescError(rc, "job rejected" if rc == ERR_REJECTED else "submit failed")
+        self._live[t.value] = spec
+        return t.value
+
+    def wait(self, ticket):
+        """(status, queued seconds, latency seconds) of a submitted job."""
+        st, q, lat = _int(), ctypes.c_double(), ctypes.c_double()
+        rc = lib().tc_pool_wait(self.h, ticket, ctypes.byref(st), ctypes.byref(q), ctypes.byref(lat))
+        if rc != OK:
+            raise TimescError(rc, "unknown ticket")
+        self._live.pop(ticket, None)
+        return st.value, q.value, lat.value
+
+    def stats(self):
+        r, q, b = _int(), _int(), ctypes.c_uint64()
+        lib().tc_pool_stats(self.h, ctypes.byref(r), ctypes.byref(q), ctypes.byref(b))
+        return dict(running=r.value, queued=q.value, held_bytes=b.value)
 
 
 def sbd_assign_noalloc(x, C, labels, dist=None, mode=MODE_COMPAT, stream=None):
