@@ -242,13 +242,161 @@ def run_reference(args, wl):
     print(json.dumps(line))
 
 
+# ---------------------------------------------------------------- many jobs (batch, serving)
+def c4_sizes(count, seed=2024):
+    """Job sizes of the batched form: n log-uniform in [64, 5e4], m log-uniform in
+    [32, 4096], k uniform in [2, 64]; job i uses generator seed i."""
+    rng = np.random.default_rng(seed)
+    n = np.exp(rng.uniform(np.log(64), np.log(5e4), count)).astype(np.int64)
+    m = np.exp(rng.uniform(np.log(32), np.log(4096), count)).astype(np.int64)
+    k = rng.integers(2, 65, count)
+    return [(int(a), int(b), int(c)) for a, b, c in zip(n, m, k)]
+
+
+def make_specs(timesc, sizes, precision, max_iter, seed0=0, noise=0.2):
+    """JobSpecs with generator data, generated on all host threads."""
+    from concurrent.futures import ThreadPoolExecutor
+
+    def one(i):
+        n, m, k = sizes[i]
+        data, _ = timesc.generate(n, m, k, noise=noise, seed=seed0 + i)
+        return timesc.JobSpec(data, k, mode=0, precision=precision, seed=seed0 + i, max_iter=max_iter)
+
+    with ThreadPoolExecutor(max_workers=host_threads()) as ex:
+        return list(ex.map(one, range(len(sizes))))
+
+
+def run_batched(args):
+    """Batched form: many independent jobs in one pool, all to convergence (or the
+    iteration cap); a step is the whole batch."""
+    import timesc
+    prec = PREC[args.precision]
+    sizes = c4_sizes(args.jobs)
+    specs = make_specs(timesc, sizes, prec, args.max_iter)
+    warm = make_specs(timesc, sorted(sizes)[: min(16, len(sizes))], prec, 2, seed0=10_000)
+    pool = timesc.Pool(device=0, workers=args.workers)
+    for _ in range(args.warmup):
+        pool.run_batch(warm)
+    clk = Clocks(0)
+    l0 = timesc.lib().tc_launch_count()
+    walls = []
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        st = pool.run_batch(specs)
+        walls.append(time.perf_counter() - t0)
+        assert all(v == timesc.OK for v in st), st
+    launches = timesc.lib().tc_launch_count() - l0
+    clocks = clk.stop()
+    pool.close()
+    wall = statistics.mean(walls)
+    iters = [s.res.iterations for s in specs]
+    pairs = sum(n * k * it for (n, m, k), it in zip(sizes, iters))
+    out = {"metric": "SBD pairs/s (batched jobs, whole k-Shape loops)", "value": pairs / wall, "unit": "pairs/s",
+           "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": wall * 1e3,
+           "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+           "dtype": "f32" if prec == 0 else args.precision, "data": "synthetic (prototype generator), seeds 0..%d"
+           % (len(sizes) - 1),
+           "config": {"workload": "batched form: %d jobs, n log-U[64,5e4], m log-U[32,4096], k U[2,64]"
+                      % len(sizes), "workers": args.workers, "max_iter": args.max_iter, "mode": "compat",
+                      "precision": args.precision, "graphs": "per-job iteration stages replayed"},
+           "jobs_per_s": len(sizes) / wall, "iterations_total": int(sum(iters)),
+           "gpu_launches": int(launches / max(args.steps, 1)), "clocks": clocks,
+           "e2e": {"value": pairs / wall, "unit": "pairs/s",
+                   "h2d_bytes_per_step": int(sum(4 * n * m for n, m, k in sizes)),
+                   "d2h_bytes_per_step": int(sum(4 * n + 4 * k * m for n, m, k in sizes)),
+                   "call": "tc_pool_run_batch (host buffers in, labels/centroids out)"}}
+    print(json.dumps(out), flush=True)
+
+
+def run_serving(args):
+    """Serving form: Poisson arrivals at 80% of the measured capacity; 95% of the
+    requests are batched-form jobs, 5% n=2e5 m=1024 k=16; HBM admission budget
+    150 GB; latency = submission to completion."""
+    import threading
+    import timesc
+    prec = PREC[args.precision]
+    rng = np.random.default_rng(7)
+    small = c4_sizes(48, seed=99)
+    lib_small = make_specs(timesc, small, prec, args.max_iter, seed0=1000)
+    big_data = [timesc.generate(200_000, 1024, 16, noise=0.2, seed=2000 + i)[0] for i in range(2)]
+    pick = ["L%d" % (i % 2) if rng.random() < 0.05 else "S%d" % rng.integers(0, len(small))
+            for i in range(args.jobs)]
+
+    def spec_for(key):
+        if key[0] == "L":
+            return timesc.JobSpec(big_data[int(key[1:])], 16, mode=0, precision=prec, seed=7, max_iter=args.max_iter)
+        src = lib_small[int(key[1:])]
+        return timesc.JobSpec(src.data, src.k, mode=0, precision=prec, seed=src.job.seed, max_iter=args.max_iter)
+
+    budget = 150 * 10**9
+    pool = timesc.Pool(device=0, workers=args.workers, hbm_budget_bytes=budget)
+    # warm-up, then capacity: a saturated batch with the request mix
+    for _ in range(max(1, args.warmup - 2)):
+        pool.run_batch([spec_for(k) for k in pick[:8]])
+    cap_keys = pick[: min(64, len(pick))]
+    t0 = time.perf_counter()
+    pool.run_batch([spec_for(k) for k in cap_keys])
+    capacity = len(cap_keys) / (time.perf_counter() - t0)
+    rate = 0.8 * capacity
+    gaps = rng.exponential(1.0 / rate, len(pick))
+    specs = [spec_for(k) for k in pick]
+    tickets = [None] * len(specs)
+    held = []
+    clk = Clocks(0)
+    start = time.perf_counter()
+
+    def producer():
+        t_next = start
+        for i, sp in enumerate(specs):
+            t_next += gaps[i]
+            d = t_next - time.perf_counter()
+            if d > 0:
+                time.sleep(d)
+            tickets[i] = pool.submit(sp)
+            held.append(pool.stats()["held_bytes"])
+
+    th = threading.Thread(target=producer)
+    th.start()
+    th.join()
+    res = [pool.wait(t) for t in tickets]
+    end = time.perf_counter()
+    clocks = clk.stop()
+    pool.close()
+    assert all(r[0] == timesc.OK for r in res), [r[0] for r in res]
+    lat = np.array([r[2] for r in res])
+    que = np.array([r[1] for r in res])
+    pairs = sum(sp.job.n * sp.job.k * sp.res.iterations for sp in specs)
+    out = {"metric": "served jobs/s at 80% load (Poisson arrivals), request latency p50/p99",
+           "value": len(specs) / (end - start), "unit": "jobs/s", "n_gpus": 1, "steps": 1, "warmup": args.warmup,
+           "ms_per_step": (end - start) * 1e3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+           "dtype": "f32" if prec == 0 else args.precision + " mixed",
+           "data": "synthetic (prototype generator)",
+           "config": {"workload": "serving form: %d requests, 95%% batched-form sizes, 5%% n=2e5 m=1024 k=16"
+                      % len(specs), "workers": args.workers, "hbm_budget_bytes": budget,
+                      "arrival_rate_per_s": rate, "measured_capacity_jobs_per_s": capacity,
+                      "max_iter": args.max_iter, "precision": args.precision},
+           "latency_s": {"p50": float(np.percentile(lat, 50)), "p99": float(np.percentile(lat, 99)),
+                         "mean": float(lat.mean()), "max": float(lat.max())},
+           "queue_s": {"p50": float(np.percentile(que, 50)), "p99": float(np.percentile(que, 99))},
+           "large_requests": int(sum(k[0] == "L" for k in pick)), "max_held_bytes": int(max(held) if held else 0),
+           "pairs_per_s": pairs / (end - start), "clocks": clocks,
+           "e2e": {"value": len(specs) / (end - start), "unit": "jobs/s",
+                   "h2d_bytes_per_step": int(sum(4 * sp.job.n * sp.job.m for sp in specs)),
+                   "d2h_bytes_per_step": int(sum(4 * sp.job.n + 4 * sp.job.k * sp.job.m for sp in specs)),
+                   "call": "tc_pool_submit / tc_pool_wait"}}
+    print(json.dumps(out), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="c3", choices=sorted(WORKLOADS))
+    ap.add_argument("--workload", default="c3", choices=sorted(WORKLOADS) + ["c4", "c5"])
+    ap.add_argument("--jobs", type=int, default=512, help="c4/c5: number of jobs")
+    ap.add_argument("--workers", type=int, default=8, help="c4/c5: jobs in flight")
+    ap.add_argument("--max-iter", type=int, default=10, help="c4/c5: k-Shape iteration cap per job")
     ap.add_argument("--precision", default="fp32", choices=sorted(PREC))
     ap.add_argument("--mode", default="compat", choices=sorted(MODES))
     ap.add_argument("--no-e2e", action="store_true")
@@ -256,6 +404,10 @@ def main():
     ap.add_argument("--no-cufft", action="store_true")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
+    if args.workload == "c4":
+        return run_batched(args)
+    if args.workload == "c5":
+        return run_serving(args)
     wl = WORKLOADS[args.workload]
     if args.impl == "reference":
         return run_reference(args, wl)
