@@ -8,6 +8,11 @@
 
 #include "tc_internal.h"
 
+std::recursive_mutex& capture_mutex() {
+    static std::recursive_mutex mu;
+    return mu;
+}
+
 namespace tc {
 
 std::atomic<uint64_t> g_launches{0};
@@ -109,6 +114,7 @@ struct StageGraph {
     }
     template <class F>
     void capture(cudaStream_t s, F&& issue) {
+        std::lock_guard<std::recursive_mutex> lk(capture_mutex());
         cudaGraph_t gr = nullptr;
         if (cudaStreamBeginCapture(s, cudaStreamCaptureModeRelaxed) != cudaSuccess) {
             cudaGetLastError();

@@ -33,6 +33,7 @@ const FftTables& fft_tables(tc_ctx* ctx, int F) {
         hN[e] = make_float2((float)std::cos(a), (float)std::sin(a));
         hF[e] = make_float2((float)std::cos(b), (float)std::sin(b));
     }
+    std::lock_guard<std::recursive_mutex> lk(capture_mutex());  // synchronous copies: not while another thread captures
     float2* dN = t->twN.as<float2>(N);
     float2* dF = t->twF.as<float2>(N);
     TC_CUDA(cudaMemcpy(dN, hN.data(), sizeof(float2) * N, cudaMemcpyHostToDevice));

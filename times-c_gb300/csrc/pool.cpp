@@ -17,6 +17,8 @@
 // first; a job larger than the whole budget is rejected at submission.
 #include <algorithm>
 #include <chrono>
+#include <cstdio>
+#include <cstdlib>
 #include <condition_variable>
 #include <deque>
 #include <mutex>
@@ -116,6 +118,8 @@ struct tc_pool {
             tc_result* res = r.result;
             lk.unlock();
             const int st = tc_kshape_run(ctx[w], job, res);
+            if (st != TC_OK && std::getenv("TIMESC_TRACE"))
+                std::fprintf(stderr, "timesc pool: job failed (%d): %s\n", st, tc_last_error(ctx[w]));
             lk.lock();
             held[w] = tc::workspace_bytes(ctx[w]);
             resv[w] = 0;

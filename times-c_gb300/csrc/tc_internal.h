@@ -4,6 +4,7 @@
 #include <cuda_runtime.h>
 
 #include <atomic>
+#include <mutex>
 #include <cstdint>
 #include <cstdio>
 #include <string>
@@ -39,12 +40,18 @@ extern std::atomic<uint64_t> g_launches;  // kernel launches issued by this libr
     } while (0)
 
 // ---------------------------------------------------------------- device buffers
+// Serialises device allocation and release with CUDA graph capture across the
+// host threads of a process: cudaFree synchronises the device, which must not
+// happen while another thread captures a stream.
+std::recursive_mutex& capture_mutex();
+
 // A grow-only device allocation owned by a context.
 struct DevBuf {
     void* p = nullptr;
     size_t bytes = 0;
     void* get(size_t need) {
         if (need <= bytes) return p;
+        std::lock_guard<std::recursive_mutex> lk(capture_mutex());
         if (p) cudaFree(p);
         p = nullptr;
         bytes = 0;
@@ -60,7 +67,9 @@ struct DevBuf {
     template <class T>
     T* as(size_t count) { return static_cast<T*>(get(count * sizeof(T))); }
     void release() {
-        if (p) cudaFree(p);
+        if (!p) return;
+        std::lock_guard<std::recursive_mutex> lk(capture_mutex());
+        cudaFree(p);
         p = nullptr;
         bytes = 0;
     }
