@@ -333,7 +333,7 @@ template <int N>
 static void centroid_spectra_n(tc_ctx* ctx, const float* C, int k, int m, float2* spec, cudaStream_t s) {
     const FftTables& tb = fft_tables(ctx, 2 * N);
     size_t sm = Cfg<N>::BUF_BYTES + sizeof(TeamScratch);
-    TC_CUDA(cudaFuncSetAttribute(k_centroid_spectra<N>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+    allow_max_dynamic_smem(k_centroid_spectra<N>);
     k_centroid_spectra<N><<<k, Plan<N>::T, sm, s>>>(C, m, (const float2*)tb.twN.p, (const float2*)tb.twF.p, spec);
     TC_CHECK_LAUNCH();
 }
@@ -341,7 +341,7 @@ static void centroid_spectra_n(tc_ctx* ctx, const float* C, int k, int m, float2
 template <int N, bool CSMEM, bool SHIFT>
 static void launch_variant(tc_ctx* ctx, const AssignParams& p, size_t sm, cudaStream_t s) {
     auto fn = k_assign_fft<N, CSMEM, SHIFT>;
-    TC_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+    allow_max_dynamic_smem(fn);
     int per_sm = 0;
     TC_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, Cfg<N>::BLOCK, sm));
     const int64_t teams_needed = (p.n + Cfg<N>::TEAMS - 1) / Cfg<N>::TEAMS;
@@ -485,7 +485,7 @@ static void noalloc_n(const NoallocDevice& d, const float* x, const float* C, in
     k_noalloc_twiddles<<<ceil_div(N, 256), 256, 0, s>>>(twN, twF, N);
     TC_CHECK_LAUNCH();
     const size_t ssm = Cfg<N>::BUF_BYTES + sizeof(TeamScratch);
-    TC_CUDA(cudaFuncSetAttribute(k_centroid_spectra<N>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ssm));
+    allow_max_dynamic_smem(k_centroid_spectra<N>);
     k_centroid_spectra<N><<<k, Plan<N>::T, ssm, s>>>(C, m, twN, twF, spec);
     TC_CHECK_LAUNCH();
     AssignParams p{};
@@ -503,7 +503,7 @@ static void noalloc_n(const NoallocDevice& d, const float* x, const float* C, in
     const bool csmem = Cfg<N>::smem(k, true) <= d.smem_optin;
     const size_t sm = Cfg<N>::smem(k, csmem);
     auto fn = csmem ? k_assign_fft<N, true, false> : k_assign_fft<N, false, false>;
-    TC_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+    allow_max_dynamic_smem(fn);
     int per_sm = 0;
     TC_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, Cfg<N>::BLOCK, sm));
     const int64_t teams = (n + Cfg<N>::TEAMS - 1) / Cfg<N>::TEAMS;

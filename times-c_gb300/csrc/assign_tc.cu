@@ -406,7 +406,7 @@ void launch_assign_tc(tc_ctx* ctx, const AssignArgs& a, int precision, cudaStrea
     p.dist_sum = a.dist_sum;
     p.err = err;
     const size_t smem = g.smem();
-    TC_CUDA(cudaFuncSetAttribute(k_assign_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    allow_max_dynamic_smem(k_assign_tc);
     const int64_t ntiles = (a.n + AT_TILE - 1) / AT_TILE;
     const int grid = (int)std::min<int64_t>(ntiles, ctx->sm_count);
     k_assign_tc<<<grid, AT_THREADS, smem, s>>>(map, p);

@@ -322,7 +322,7 @@ void extract_async(tc_ctx* ctx, const ExtractArgs& a, cudaStream_t s) {
     TC_CHECK_LAUNCH();
     if (n > 0) {
         size_t smem = (size_t)9 * k * sizeof(int);
-        TC_CUDA(cudaFuncSetAttribute(k_seg_scatter, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        allow_max_dynamic_smem(k_seg_scatter);
         k_seg_scatter<<<nchunks, SEG_BLOCK, smem, s>>>(a.labels, n, k, chunk, offsets, perm);
         TC_CHECK_LAUNCH();
     }

@@ -324,7 +324,7 @@ __global__ void __launch_bounds__(PC_THREADS, 1) k_power_cluster(PowerClusterPar
 template <int CL, int BPL>
 static void launch_cluster(const PowerClusterParams& pp, int k, size_t smem, cudaStream_t s) {
     auto kern = k_power_cluster<CL, BPL>;
-    TC_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    allow_max_dynamic_smem(kern);
     if (CL > 8) TC_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3((unsigned)k * CL);

@@ -28,16 +28,35 @@ struct TcError {
 namespace tc {
 extern std::atomic<uint64_t> g_launches;  // kernel launches issued by this library
 }
-#define TC_CHECK_LAUNCH()                 \
-    do {                                  \
-        ::tc::g_launches.fetch_add(1);    \
-        TC_CUDA(cudaGetLastError());      \
+// after a kernel launch: counts it, and names the launch site in the error
+#define TC_CHECK_LAUNCH()                                                                        \
+    do {                                                                                         \
+        ::tc::g_launches.fetch_add(1);                                                           \
+        cudaError_t e_ = cudaGetLastError();                                                     \
+        if (e_ != cudaSuccess)                                                                   \
+            throw TcError{TC_ERR_CUDA, std::string("kernel launch at ") + __FILE__ + ":" +        \
+                                           std::to_string(__LINE__) + ": " + cudaGetErrorString(e_)}; \
     } while (0)
 
 #define TC_REQUIRE(cond, code, text)                         \
     do {                                                     \
         if (!(cond)) throw TcError{(code), std::string(text)}; \
     } while (0)
+
+// Raise a kernel's dynamic shared memory limit to the device maximum.  Every call
+// sets the same value: host threads that launch one kernel with different sizes
+// must never lower the limit under a launch, or a replayed CUDA graph, that
+// needs more (a kernel run with less shared memory than it addresses faults).
+template <class K>
+inline void allow_max_dynamic_smem(K kernel) {
+    cudaFuncAttributes fa;
+    TC_CUDA(cudaFuncGetAttributes(&fa, kernel));
+    int dev = 0, optin = 0;
+    TC_CUDA(cudaGetDevice(&dev));
+    TC_CUDA(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
+    TC_CUDA(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 optin - (int)fa.sharedSizeBytes));
+}
 
 // ---------------------------------------------------------------- device buffers
 // Serialises device allocation and release with CUDA graph capture across the

@@ -301,13 +301,13 @@ void launch_gram_tc(tc_ctx* ctx, const float* seg, const int32_t* counts, const 
     const int nt = ceil_div(m, GT_TILE);
     dim3 grid(nt * (nt + 1) / 2, k);
     if (fmt == 1) {
-        TC_CUDA(cudaFuncSetAttribute(k_gram_tc<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, GtCfg<1>::SMEM));
+        allow_max_dynamic_smem(k_gram_tc<1>);
         k_gram_tc<1><<<grid, 128, GtCfg<1>::SMEM, s>>>(map, map_lo, counts, poff, m, ld, nt, S, err);
     } else if (fmt == 2) {
-        TC_CUDA(cudaFuncSetAttribute(k_gram_tc<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, GtCfg<2>::SMEM));
+        allow_max_dynamic_smem(k_gram_tc<2>);
         k_gram_tc<2><<<grid, 128, GtCfg<2>::SMEM, s>>>(map, map_lo, counts, poff, m, ld, nt, S, err);
     } else {
-        TC_CUDA(cudaFuncSetAttribute(k_gram_tc<3>, cudaFuncAttributeMaxDynamicSharedMemorySize, GtCfg<3>::SMEM));
+        allow_max_dynamic_smem(k_gram_tc<3>);
         k_gram_tc<3><<<grid, 128, GtCfg<3>::SMEM, s>>>(map, map_lo, counts, poff, m, ld, nt, S, err);
     }
     TC_CHECK_LAUNCH();
