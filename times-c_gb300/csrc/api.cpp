@@ -197,7 +197,7 @@ static LoopState run_loop(tc_ctx* ctx, const tc_job* job, const float* x, int k,
     } h;
     static_assert(sizeof(h) == 56, "aux layout");
     StageGraph g_extract, g_assign;
-    const bool graphs = !std::getenv("TIMESC_NO_GRAPHS");
+    const bool graphs = ctx->graphs && !std::getenv("TIMESC_NO_GRAPHS");
     auto readback = [&]() {
         TC_CUDA(cudaMemcpyAsync(&h, aux, sizeof(h), cudaMemcpyDeviceToHost, s));
         TC_CUDA(cudaStreamSynchronize(s));
