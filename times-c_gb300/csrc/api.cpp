@@ -13,6 +13,12 @@ std::recursive_mutex& capture_mutex() {
     return mu;
 }
 
+size_t guard_bytes(size_t need) {
+    static const bool on = std::getenv("TIMESC_GUARD") != nullptr;
+    // a multiple of 4 KB: the buffer after the front zone keeps cudaMalloc's alignment
+    return on ? (((size_t)1 << 20) + need / 4 + 4095) / 4096 * 4096 : 0;
+}
+
 namespace tc {
 
 std::atomic<uint64_t> g_launches{0};
@@ -228,6 +234,7 @@ static LoopState run_loop(tc_ctx* ctx, const tc_job* job, const float* x, int k,
     auto do_assign = [&]() -> bool {
         g_assign.run(graphs, s, issue_assign);
         readback();
+        check_guards(ctx, "assignment");
         st.inertia = h.dsum / (double)n;
         return h.changed == 0;
     };
@@ -248,6 +255,7 @@ static LoopState run_loop(tc_ctx* ctx, const tc_job* job, const float* x, int k,
     auto extract = [&]() {
         g_extract.run(graphs, s, issue_extract);
         readback();
+        check_guards(ctx, "extraction");
         TC_REQUIRE(h.bad_label == 0, TC_ERR_ARG, "a label is outside [0, k)");
         if (!cal_select) st.sum_class = h.sum_class;  // get_class_centers_a leaves sum_class alone
     };
@@ -269,6 +277,40 @@ static LoopState run_loop(tc_ctx* ctx, const tc_job* job, const float* x, int k,
         }
     }
     return st;
+}
+
+static const char* const WS_NAMES[] = {"x", "labels", "old_labels", "shift", "dist", "centroids", "spectra",
+                                       "seg", "perm", "chunk_counts", "counts", "offsets", "gate", "scal",
+                                       "gram", "rowsum", "gram_yt", "gram_poff", "piter", "pstats", "aux",
+                                       "toeplitz", "toeplitz_norm", "xbf", "xbf_norm"};
+
+static std::vector<DevBuf*> workspace_buffers(tc_ctx* ctx);
+
+void check_guards(tc_ctx* ctx, const char* where) {
+    if (!guard_bytes(1)) return;
+    TC_CUDA(cudaStreamSynchronize(ctx->own_stream));
+    auto check = [&](const DevBuf* b, const std::string& name) {
+        if (!b->p) return;
+        const size_t g = guard_bytes(b->bytes);
+        std::vector<unsigned char> h(g);
+        for (int side = 0; side < 2; ++side) {
+            const char* z = side ? static_cast<const char*>(b->p) + b->bytes : static_cast<const char*>(b->base());
+            TC_CUDA(cudaMemcpy(h.data(), z, g, cudaMemcpyDeviceToHost));
+            for (size_t i = 0; i < g; ++i)
+                if (h[i] != GUARD_BYTE) {
+                    std::fprintf(stderr, "timesc guard: buffer %s (%zu bytes) overwritten %s at %zu after %s\n",
+                                 name.c_str(), b->bytes, side ? "after its end" : "before its start",
+                                 side ? i : g - i, where);
+                    throw TcError{TC_ERR_CUDA, "guard of buffer " + name + " overwritten after " + where};
+                }
+        }
+    };
+    const auto bufs = workspace_buffers(ctx);
+    for (size_t i = 0; i < bufs.size(); ++i) check(bufs[i], WS_NAMES[i]);
+    for (const FftTables* t : ctx->fft) {
+        check(&t->twN, "twN" + std::to_string(t->F));
+        check(&t->twF, "twF" + std::to_string(t->F));
+    }
 }
 
 static std::vector<DevBuf*> workspace_buffers(tc_ctx* ctx) {

@@ -64,6 +64,12 @@ inline void allow_max_dynamic_smem(K kernel) {
 // happen while another thread captures a stream.
 std::recursive_mutex& capture_mutex();
 
+// Diagnostics (TIMESC_GUARD set): every buffer gets a guard zone after its end,
+// filled with GUARD_BYTE, which check_guards() verifies - a kernel writing past
+// a buffer then changes the guard instead of another allocation.
+constexpr unsigned char GUARD_BYTE = 0xA5;
+size_t guard_bytes(size_t need);  // 0 unless diagnostics are on
+
 // A grow-only device allocation owned by a context.
 struct DevBuf {
     void* p = nullptr;
@@ -71,24 +77,33 @@ struct DevBuf {
     void* get(size_t need) {
         if (need <= bytes) return p;
         std::lock_guard<std::recursive_mutex> lk(capture_mutex());
-        if (p) cudaFree(p);
+        if (p) cudaFree(base());
         p = nullptr;
         bytes = 0;
         if (need == 0) return nullptr;
-        cudaError_t e = cudaMalloc(&p, need);
+        const size_t g = guard_bytes(need);
+        cudaError_t e = cudaMalloc(&p, need + 2 * g);
         if (e != cudaSuccess) {
             cudaGetLastError();
+            p = nullptr;
             throw TcError{TC_ERR_NOMEM, "cudaMalloc of " + std::to_string(need) + " bytes failed"};
+        }
+        if (g) {  // guard zones before and after the buffer; the buffer itself poisoned
+            cudaMemset(p, GUARD_BYTE, g);
+            p = static_cast<char*>(p) + g;
+            cudaMemset(static_cast<char*>(p) + need, GUARD_BYTE, g);
+            cudaMemset(p, 0xFF, need);  // NaN floats, -1 integers: reads before writes show up
         }
         bytes = need;
         return p;
     }
+    void* base() const { return p ? static_cast<char*>(p) - guard_bytes(bytes) : nullptr; }
     template <class T>
     T* as(size_t count) { return static_cast<T*>(get(count * sizeof(T))); }
     void release() {
         if (!p) return;
         std::lock_guard<std::recursive_mutex> lk(capture_mutex());
-        cudaFree(p);
+        cudaFree(base());
         p = nullptr;
         bytes = 0;
     }
@@ -193,6 +208,9 @@ int run_extract(tc_ctx* ctx, const ExtractArgs& a, cudaStream_t s);
 // workspace of a context: free every buffer (the context must be idle) / bytes held
 void release_workspace(tc_ctx* ctx);
 size_t workspace_bytes(tc_ctx* ctx);
+// with TIMESC_GUARD: synchronise the context's stream and throw if a buffer's
+// guard zone changed (names the buffer and `where`)
+void check_guards(tc_ctx* ctx, const char* where);
 
 // helpers
 inline int ceil_div(int64_t a, int64_t b) { return (int)((a + b - 1) / b); }
