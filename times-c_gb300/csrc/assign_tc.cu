@@ -231,6 +231,16 @@ __global__ void __launch_bounds__(AT_THREADS, 1) k_assign_tc(const __grid_consta
                 const int64_t uses = (q + 1 - s) / 2;  // loads issued into stage s
                 if (uses > 0) sm100::mbar_wait(&b_full[s], (int)((uses - 1) & 1), p.err);
             }
+            // likewise the MMA thread's last commits (they arrive when their MMAs end):
+            // no arrival may land in this CTA's shared memory after it has left, when
+            // another kernel's CTA may own it
+            if (ok) {
+                for (int s = 0; s < 2; ++s) {
+                    const int64_t uses = (q + 1 - s) / 2;
+                    if (uses > 0) sm100::mbar_wait(&b_empty[s], (int)((uses - 1) & 1), p.err);
+                }
+                if (lt > 0) sm100::mbar_wait(&a_empty, (lt - 1) & 1, p.err);
+            }
         }
         __syncwarp();
     } else if (warp == 1) {

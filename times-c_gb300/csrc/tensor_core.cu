@@ -180,6 +180,12 @@ __global__ void __launch_bounds__(128, 1) k_gram_tc(const __grid_constant__ CUte
                 sm100::tma_load_2d(A + 3 * GT_TILE_BYTES, &tmap_lo, x0 + kb * KE, tb * GT_TILE, &full[s]);
             }
         }
+        // the MMA thread's last commits to empty[] arrive when their MMAs end: wait for
+        // them, so no arrival lands in this CTA's shared memory after it has left
+        // (another kernel's CTA may own it by then)
+        if (ok)
+            for (int kb = nk > G::STAGES ? nk - G::STAGES : 0; kb < nk; ++kb)
+                sm100::mbar_wait(&empty[kb % G::STAGES], (kb / G::STAGES) & 1, err);
     } else if (warp == 1 && lane == 0) {
         // MMA issuer
         constexpr uint32_t ID = sm100::idesc(FMT == 1 ? 1 : 2, 128, 128);
