@@ -144,9 +144,7 @@ struct tc_ctx {
     std::vector<FftTables*> fft;  // cached per F
     Workspace ws;
     cudaStream_t own_stream = nullptr;
-    // iteration stages replayed from CUDA graphs (off for the pool's workers: with
-    // several host threads issuing work, stream capture in one thread while others
-    // launch, copy and synchronise gave wrong results and memory faults here)
+    // iteration stages replayed from CUDA graphs
     bool graphs = true;
     // series whose BF16 copy and norms sit in ws.xbf / ws.xbf_norm (tc_prepare_series)
     const float* prep_x = nullptr;
