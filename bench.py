@@ -300,7 +300,7 @@ def run_batched(args):
            % (len(sizes) - 1),
            "config": {"workload": "batched form: %d jobs, n log-U[64,5e4], m log-U[32,4096], k U[2,64]"
                       % len(sizes), "workers": args.workers, "max_iter": args.max_iter, "mode": "compat",
-                      "precision": args.precision, "graphs": "off in pool workers (stages issued directly)"},
+                      "precision": args.precision, "graphs": "per-job iteration stages replayed"},
            "jobs_per_s": len(sizes) / wall, "iterations_total": int(sum(iters)),
            "gpu_launches": int(launches / max(args.steps, 1)), "clocks": clocks,
            "e2e": {"value": pairs / wall, "unit": "pairs/s",

@@ -155,6 +155,8 @@ __global__ void __launch_bounds__(SEG_BLOCK) k_seg_scatter(const int32_t* __rest
             for (int w = 0; w < 8; ++w) add += wcnt[w * k + j];
             running[j] += add;
         }
+        // the next pass zeroes wcnt: every thread must have read it first
+        __syncthreads();
     }
 }
 

@@ -3,11 +3,10 @@
 // process, Code/test/test_kshape.cu).
 //
 // Each worker is a context (its own stream and workspace) driven by its own host
-// thread, so jobs of different sizes overlap on the device: a small job's stages
-// fill the SMs a large job's stages leave idle, and no job waits for another's
-// host synchronisations.  Workers issue their stages directly: CUDA graph capture
-// in one thread while the others issued work gave wrong results and GPU memory
-// faults, so graphs are kept to single-context runs (tc_kshape_run).
+// thread; the loop of each job replays its iteration stages from CUDA graphs, so
+// jobs of different sizes overlap on the device: a small job's stages fill the
+// SMs a large job's stages leave idle, and no job waits for another's host
+// synchronisations.
 //
 // Admission keeps the bytes held by the workers' workspaces (grow-only device
 // buffers) within the budget.  A running job may grow its worker's buffers by up
@@ -223,7 +222,6 @@ int tc_pool_create(int device, const tc_pool_opts* opts, tc_pool** out) {
             delete p;
             return st;
         }
-        c->graphs = false;  // see tc_ctx::graphs
         p->ctx.push_back(c);
     }
     p->held.assign(workers, 0);

@@ -325,6 +325,7 @@ template <int CL, int BPL>
 static void launch_cluster(const PowerClusterParams& pp, int k, size_t smem, cudaStream_t s) {
     auto kern = k_power_cluster<CL, BPL>;
     allow_max_dynamic_smem(kern);
+    if (CL > 8) TC_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3((unsigned)k * CL);
     cfg.blockDim = dim3(PC_THREADS);
@@ -354,13 +355,11 @@ void power_eigvecs(tc_ctx* ctx, const float* S, int ld, const double* r, const d
                    cudaStream_t s) {
     int* steps = ctx->ws.pstats.as<int>((size_t)k);
     PowerClusterParams pp{S, ld, r, tot, counts, offsets, seg, C, k, m, tmax, mode, tol * tol, steps};
-    // Portable 8-CTA clusters for every length.  Non-portable 16-CTA clusters (tried
-    // for m > 1024) faulted the GPU (Xid 31) when other jobs' kernels ran beside
-    // them in the worker pool, and never alone.
+    // long series stream tens of MB per step from HBM: spread each over 16 SMs
     if (m > 1024) {
-        const size_t smem = cluster_smem<8>(m, ld);
+        const size_t smem = cluster_smem<16>(m, ld);
         TC_REQUIRE(smem + 4096 <= ctx->smem_optin, TC_ERR_UNSUPPORTED, "power iteration: series too long");
-        launch_cluster<8, 0>(pp, k, smem, s);
+        launch_cluster<16, 0>(pp, k, smem, s);
     } else {
         const int nv4 = ld / 4;
         const size_t smem = cluster_smem<8>(m, ld);

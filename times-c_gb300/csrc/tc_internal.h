@@ -144,9 +144,7 @@ struct tc_ctx {
     std::vector<FftTables*> fft;  // cached per F
     Workspace ws;
     cudaStream_t own_stream = nullptr;
-    // iteration stages replayed from CUDA graphs (off for the pool's workers: stream
-    // capture in one host thread while others launched, copied and synchronised gave
-    // wrong results and GPU memory faults (Xid 31) in the pool; alone it is exact)
+    // iteration stages replayed from CUDA graphs
     bool graphs = true;
     // series whose BF16 copy and norms sit in ws.xbf / ws.xbf_norm (tc_prepare_series)
     const float* prep_x = nullptr;
