@@ -2,9 +2,12 @@
 
 Workload (default): the precision configuration of the Times-C baseline,
 n = 1,000,000 series, m = 512, k = 32, synthetic data (the prototype generator
-of times-c_gb300/csrc/gen.cpp, noise 0.3).  A step is one whole k-Shape
-iteration in the reference's loop order (extract shapes -> SBD assignment ->
-convergence read-back) over all series, with the series resident in HBM.
+of times-c_gb300/csrc/gen.cpp, noise 0.3), in the mixed-precision form (BF16
+tensor-core correlation and Gram, FP32 accumulation); the plain FP32 form runs
+beside it on the same series and the line reports both and how far apart their
+results are.  A step is one whole k-Shape iteration in the reference's loop order
+(extract shapes -> SBD assignment -> convergence read-back) over all series,
+with the series resident in HBM.
 
   value      SBD pairs/s = n*k / (iteration time), whole iterations
   e2e        the same through tc_kshape_run with pinned host buffers
@@ -249,6 +252,77 @@ def run_reference(args, wl):
     print(json.dumps(line))
 
 
+def ari(a, b):
+    """Adjusted Rand index of two labelings (contingency table in numpy)."""
+    a = np.asarray(a, np.int64)
+    b = np.asarray(b, np.int64)
+    nb = int(b.max()) + 1
+    cont = np.bincount(a * nb + b, minlength=(int(a.max()) + 1) * nb).reshape(-1, nb).astype(np.float64)
+    c2 = lambda v: v * (v - 1) / 2.0
+    s_ij, s_a, s_b = c2(cont).sum(), c2(cont.sum(1)).sum(), c2(cont.sum(0)).sum()
+    exp = s_a * s_b / c2(float(len(a)))
+    mx = 0.5 * (s_a + s_b)
+    return 1.0 if mx == exp else float((s_ij - exp) / (mx - exp))
+
+
+def plain_fp32_compare(ctx, x, labels, C, n, m, k, mode, prec, stream, ms_mixed, a_ms_mixed, steps=2):
+    """Times the plain FP32 form on the same series and state (whole iterations and the
+    assignment alone), and measures how far the mixed form is from it over all n: one
+    extraction and one assignment from the same labels in both forms (centroid error,
+    distance error, label agreement and ARI)."""
+    import torch
+    lab0 = labels.clone()
+    C32 = torch.empty_like(C)
+    C16 = torch.empty_like(C)
+    ctx.extract_shapes(x, lab0, C32, mode=mode, precision=PREC["fp32"])
+    ctx.extract_shapes(x, lab0, C16, mode=mode, precision=prec)
+    l32 = torch.empty_like(labels)
+    l16 = torch.empty_like(labels)
+    d32 = torch.empty((n,), dtype=torch.float32, device="cuda")
+    d16 = torch.empty_like(d32)
+    ctx.sbd_assign(x, C32, mode=mode, precision=PREC["fp32"], labels=l32, dist=d32)
+    ctx.sbd_assign(x, C32, mode=mode, precision=prec, labels=l16, dist=d16)
+    torch.cuda.synchronize()
+    L32, L16 = l32.cpu().numpy(), l16.cpu().numpy()
+    rep = {"centroid_max_abs_err": float((C16 - C32).abs().max().item()),
+           "sbd_max_abs_err": float((d16 - d32).abs().max().item()),
+           "label_agreement": float((L32 == L16).mean()), "ari": ari(L32, L16),
+           "what": "mixed vs plain FP32 over all n: extraction from the same labels, assignment against "
+                   "the same FP32 centroids (the FP32 form is parity-tested against the FP64 oracle)"}
+    # timing: whole iterations and the assignment in FP32
+    e0, e1, a0, a1 = (torch.cuda.Event(enable_timing=True) for _ in range(4))
+    lab = lab0.clone()
+    old = lab0.clone()
+    ch = torch.zeros(1, dtype=torch.int32, device="cuda")
+    ds = torch.zeros(1, dtype=torch.float64, device="cuda")
+    dist = torch.empty_like(d32)
+    for _ in range(2):  # warm
+        ctx.extract_shapes(x, lab, C32, mode=mode, precision=PREC["fp32"])
+        ctx.sbd_assign(x, C32, mode=mode, precision=PREC["fp32"], labels=lab, dist=dist)
+    torch.cuda.synchronize()
+    a_tot = 0.0
+    e0.record(stream)
+    for _ in range(steps):
+        ctx.extract_shapes(x, lab, C32, mode=mode, precision=PREC["fp32"])
+        ch.zero_()
+        ds.zero_()
+        a0.record(stream)
+        ctx.sbd_assign(x, C32, mode=mode, precision=PREC["fp32"], labels=lab, dist=dist, old_labels=old,
+                       changed=ch, dist_sum=ds)
+        a1.record(stream)
+        ch.item()
+        a_tot += a0.elapsed_time(a1)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms32 = e0.elapsed_time(e1) / steps
+    a32 = a_tot / steps
+    rep.update({"ms_per_iteration": ms32, "assign_ms": a32, "assign_pairs_per_s": n * k / (a32 / 1e3),
+                "pairs_per_s_whole_iterations": n * k / (ms32 / 1e3),
+                "mixed_vs_plain_fp32_assign_speedup": a32 / a_ms_mixed,
+                "mixed_vs_plain_fp32_iteration_speedup": ms32 / ms_mixed})
+    return rep
+
+
 # ---------------------------------------------------------------- many jobs (batch, serving)
 def c4_sizes(count, seed=2024):
     """Job sizes of the batched form: n log-uniform in [64, 5e4], m log-uniform in
@@ -406,7 +480,9 @@ def main():
     ap.add_argument("--jobs", type=int, default=512, help="c4/c5: number of jobs")
     ap.add_argument("--workers", type=int, default=8, help="c4/c5: jobs in flight")
     ap.add_argument("--max-iter", type=int, default=10, help="c4/c5: k-Shape iteration cap per job")
-    ap.add_argument("--precision", default="fp32", choices=sorted(PREC))
+    ap.add_argument("--precision", default="bf16", choices=sorted(PREC),
+                    help="c3 default: the precision form (BF16 tensor-core correlation and Gram); the plain "
+                         "FP32 form is timed beside it")
     ap.add_argument("--mode", default="compat", choices=sorted(MODES))
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
@@ -539,6 +615,11 @@ def main():
                "kshape_iters_per_s": 1e3 / ms_step,
                "assign_pairs_per_s": n * k / (a_ms / 1e3),
                "roofline": roof, "gpu_launches": int(launches), "clocks": clocks}
+
+    # the plain FP32 form on the same series, and the mixed form's agreement with it
+    if out is not None and prec != PREC["fp32"]:
+        out["plain_fp32_fused"] = plain_fp32_compare(ctx, x, labels, C, n, m, k, mode, prec, stream,
+                                                     ms_step, a_ms)
 
     # library baseline: the reference's cuFFT formulation in plain FP32
     if out is not None and not args.no_cufft:
