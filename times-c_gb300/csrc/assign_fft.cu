@@ -9,7 +9,10 @@
 // shift) per series reach HBM.
 #include <curand_kernel.h>
 
+#include <algorithm>
 #include <cmath>
+#include <cstdio>
+#include <cstdlib>
 #include <mutex>
 
 #include "sbd_core.cuh"
@@ -338,15 +341,98 @@ static void centroid_spectra_n(tc_ctx* ctx, const float* C, int k, int m, float2
     TC_CHECK_LAUNCH();
 }
 
+// A launch plan of the fused assignment: centroid spectra staged in shared memory
+// or read through L1, and how many blocks per SM the grid is sized for (the
+// kernel loops over series, so fewer blocks means fewer, longer-lived teams).
+struct AssignPlan {
+    bool csmem;
+    int blocks_per_sm;  // 0: the occupancy maximum
+};
+
 template <int N, bool CSMEM, bool SHIFT>
-static void launch_variant(tc_ctx* ctx, const AssignParams& p, size_t sm, cudaStream_t s) {
+static void launch_variant(tc_ctx* ctx, const AssignParams& p, int blocks_per_sm, cudaStream_t s) {
     auto fn = k_assign_fft<N, CSMEM, SHIFT>;
     allow_max_dynamic_smem(fn);
+    const size_t sm = Cfg<N>::smem(p.k, CSMEM);
     int per_sm = 0;
     TC_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, Cfg<N>::BLOCK, sm));
+    per_sm = std::max(per_sm, 1);
+    if (blocks_per_sm > 0) per_sm = std::min(per_sm, blocks_per_sm);
     const int64_t teams_needed = (p.n + Cfg<N>::TEAMS - 1) / Cfg<N>::TEAMS;
-    const int grid = (int)std::min<int64_t>(teams_needed, (int64_t)ctx->sm_count * std::max(per_sm, 1));
+    const int grid = (int)std::min<int64_t>(teams_needed, (int64_t)ctx->sm_count * per_sm);
     fn<<<grid, Cfg<N>::BLOCK, sm, s>>>(p);
+}
+
+template <int N, bool SHIFT>
+static void launch_plan(tc_ctx* ctx, const AssignParams& p, const AssignPlan& pl, cudaStream_t s) {
+    if (pl.csmem) launch_variant<N, true, SHIFT>(ctx, p, pl.blocks_per_sm, s);
+    else launch_variant<N, false, SHIFT>(ctx, p, pl.blocks_per_sm, s);
+}
+
+// Autotuner: the first assignment of a shape (FFT length, k, shift output) on a
+// context times every candidate plan on a sample of its own series (outputs for the
+// sample rows are overwritten by the real launch that follows; no counters are
+// touched) and keeps the fastest for the context's later launches, graph captures
+// included.  Candidates: spectra in shared memory (when they fit) or not, times
+// the occupancy maximum, half of it and one block per SM.  Off with TIMESC_AUTOTUNE=0,
+// and never inside a stream capture (the default plan is used then).
+template <int N, bool SHIFT>
+static AssignPlan tuned_plan(tc_ctx* ctx, const AssignParams& p, cudaStream_t s) {
+    const bool fits = Cfg<N>::smem(p.k, true) <= ctx->smem_optin;
+    const AssignPlan dflt{fits, 0};
+    const uint64_t key = ((uint64_t)N << 40) | ((uint64_t)p.k << 8) | (SHIFT ? 1u : 0u);
+    for (const auto& t : ctx->tuned)
+        if (t.first == key) return AssignPlan{(t.second & 1u) != 0, (int)(t.second >> 1)};
+    const char* env = std::getenv("TIMESC_AUTOTUNE");
+    cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+    TC_CUDA(cudaStreamIsCapturing(s, &cap));
+    const int64_t sample = std::min<int64_t>(p.n, (int64_t)ctx->sm_count * Cfg<N>::TEAMS * 8);
+    if ((env && env[0] == '0') || cap != cudaStreamCaptureStatusNone || sample < (int64_t)ctx->sm_count * 4)
+        return dflt;
+    AssignParams q = p;
+    q.n = sample;
+    q.changed = nullptr;
+    q.dist_sum = nullptr;
+    std::vector<AssignPlan> cands;
+    for (int cs = fits ? 1 : 0; cs >= 0; --cs)
+        for (int b : {0, -2, 1}) cands.push_back(AssignPlan{cs != 0, b});
+    cudaEvent_t e0, e1;
+    TC_CUDA(cudaEventCreate(&e0));
+    TC_CUDA(cudaEventCreate(&e1));
+    float best = 3.0e38f;
+    AssignPlan pick = dflt;
+    for (AssignPlan c : cands) {
+        if (c.blocks_per_sm == -2) {  // half the occupancy maximum
+            int per_sm = 0;
+            if (c.csmem)
+                TC_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_assign_fft<N, true, SHIFT>,
+                                                                      Cfg<N>::BLOCK, Cfg<N>::smem(p.k, true)));
+            else
+                TC_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_assign_fft<N, false, SHIFT>,
+                                                                      Cfg<N>::BLOCK, Cfg<N>::smem(p.k, false)));
+            if (per_sm < 2) continue;
+            c.blocks_per_sm = per_sm / 2;
+        }
+        launch_plan<N, SHIFT>(ctx, q, c, s);  // warm
+        TC_CUDA(cudaEventRecord(e0, s));
+        for (int r = 0; r < 2; ++r) launch_plan<N, SHIFT>(ctx, q, c, s);
+        TC_CUDA(cudaEventRecord(e1, s));
+        TC_CUDA(cudaEventSynchronize(e1));
+        TC_CUDA(cudaGetLastError());
+        float ms = 0.f;
+        TC_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+        if (ms < best) {
+            best = ms;
+            pick = c;
+        }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    ctx->tuned.emplace_back(key, (uint32_t)(pick.csmem ? 1 : 0) | ((uint32_t)pick.blocks_per_sm << 1));
+    if (std::getenv("TIMESC_TRACE"))
+        std::fprintf(stderr, "timesc: autotune assignment F=%d k=%d shift=%d -> spectra %s, %d blocks/SM\n",
+                     2 * N, p.k, (int)SHIFT, pick.csmem ? "in shared memory" : "through L1", pick.blocks_per_sm);
+    return pick;
 }
 
 template <int N>
@@ -370,16 +456,9 @@ static void assign_n(tc_ctx* ctx, const AssignArgs& a, cudaStream_t s) {
     p.old_labels = a.old_labels;
     p.changed = a.changed;
     p.dist_sum = a.dist_sum;
-    bool csmem = Cfg<N>::smem(a.k, true) <= ctx->smem_optin;
-    size_t sm = Cfg<N>::smem(a.k, csmem);
     const bool want_shift = a.shift != nullptr || a.fixed != nullptr;
-    if (csmem) {
-        if (want_shift) launch_variant<N, true, true>(ctx, p, sm, s);
-        else launch_variant<N, true, false>(ctx, p, sm, s);
-    } else {
-        if (want_shift) launch_variant<N, false, true>(ctx, p, sm, s);
-        else launch_variant<N, false, false>(ctx, p, sm, s);
-    }
+    if (want_shift) launch_plan<N, true>(ctx, p, tuned_plan<N, true>(ctx, p, s), s);
+    else launch_plan<N, false>(ctx, p, tuned_plan<N, false>(ctx, p, s), s);
     TC_CHECK_LAUNCH();
 }
 

@@ -146,6 +146,8 @@ struct tc_ctx {
     cudaStream_t own_stream = nullptr;
     // iteration stages replayed from CUDA graphs
     bool graphs = true;
+    // launch plans picked by the autotuner, per kernel shape (see assign_fft.cu)
+    std::vector<std::pair<uint64_t, uint32_t>> tuned;
     // series whose BF16 copy and norms sit in ws.xbf / ws.xbf_norm (tc_prepare_series)
     const float* prep_x = nullptr;
     int64_t prep_n = 0;
