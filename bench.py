@@ -480,15 +480,17 @@ def main():
     ap.add_argument("--jobs", type=int, default=512, help="c4/c5: number of jobs")
     ap.add_argument("--workers", type=int, default=8, help="c4/c5: jobs in flight")
     ap.add_argument("--max-iter", type=int, default=10, help="c4/c5: k-Shape iteration cap per job")
-    ap.add_argument("--precision", default="bf16", choices=sorted(PREC),
-                    help="c3 default: the precision form (BF16 tensor-core correlation and Gram); the plain "
-                         "FP32 form is timed beside it")
+    ap.add_argument("--precision", default=None, choices=sorted(PREC),
+                    help="default per workload: c3 and c5 the mixed-precision form (bf16; for c3 the plain FP32 "
+                         "form is timed beside it), c1, c2 and c4 fp32")
     ap.add_argument("--mode", default="compat", choices=sorted(MODES))
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-cufft", action="store_true")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
+    if args.precision is None:
+        args.precision = "bf16" if args.workload in ("c3", "c3s", "c5") else "fp32"
     if args.workload == "c4":
         return run_batched(args)
     if args.workload == "c5":
