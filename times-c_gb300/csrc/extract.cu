@@ -5,16 +5,17 @@
 //             (warp match + per-warp counts) - replaces class_count/get_loc2
 //             (a single-thread loop for n < 1e6) and block_alloc2D (:21-188).
 //   gate      per-cluster alignment gate (:1129-1135).
-//   gather    align + re-z-normalise members into cluster order (znorm.cu).
-//   Gram      S_c = sum_{i in c} y_i y_i^T (:532-537), SIMT FP32 here; the
-//             tensor-core version lives in gram_tc.cu.
+//   gather    align + re-z-normalise members into cluster order (znorm.cu);
+//             with the tensor-core Gram (m <= 1024) written straight into its
+//             transposed, cluster-padded operand.
+//   Gram      S_c = sum_{i in c} y_i y_i^T (:532-537): tcgen05 (tensor_core.cu,
+//             3xTF32 for the FP32 form) or SIMT FP32 here.
 //   centring  M = Q S Q is never formed: M v = S v - (1.v/m) r - (r.v/m) 1
 //             + (tot 1.v/m^2) 1 with r = S 1, tot = 1^T S 1 (replaces get_matQ and
 //             two in-place m^3 GEMMs, :204-214, :551-570).
-//   power     power.cu: all clusters in one cooperative launch, with the
-//             Rayleigh quotient, the step difference and the norms in FP64
-//             (:269-360, :577-630); the sign rule and the store are fused into
-//             the final kernel (get_center, :217-264).
+//   power     power.cu: one thread-block cluster per k-Shape cluster, all in one
+//             launch (:269-360, :577-630); the Rayleigh quotient, the sign rule and
+//             the store are fused into its last step (get_center, :217-264).
 #include <algorithm>
 #include <cmath>
 
@@ -282,7 +283,8 @@ __global__ void k_rowsum_total(const double* __restrict__ r, const int32_t* __re
 }
 
 void power_eigvecs(tc_ctx* ctx, const float* S, int ld, const double* r, const double* tot, const int32_t* counts,
-                   const int32_t* offsets, const float* seg, int k, int m, int mode, int tmax, double tol, float* C,
+                   const int32_t* offsets, const float* seg, bool lead_rows, int k, int m, int mode, int tmax,
+                   double tol, float* C,
                    cudaStream_t s);
 
 // ---------------------------------------------------------------- driver
@@ -304,7 +306,7 @@ void extract_async(tc_ctx* ctx, const ExtractArgs& a, cudaStream_t s) {
     int64_t* poff = ws.gram_poff.as<int64_t>(k);
     uint8_t* gate = ws.gate.as<uint8_t>(k);
     int32_t* scal = ws.scal.as<int32_t>(16);
-    float* seg = ws.seg.as<float>((size_t)std::max<int64_t>(n, 1) * m);
+    float* seg = nullptr;  // row-major members in cluster order (only without the fused gather)
     const int ld = (m + 3) & ~3;  // Gram row pitch: rows stream as float4
     float* S = ws.gram.as<float>((size_t)k * m * ld);
     double* rs = ws.rowsum.as<double>((size_t)k * m + k);
@@ -352,14 +354,29 @@ void extract_async(tc_ctx* ctx, const ExtractArgs& a, cudaStream_t s) {
         launch_assign_fft(ctx, aa, s);
         shift = sh;
     }
-    launch_gather_norm(a.x, perm, a.labels, shift, gate, n, m, seg, ctx->sm_count, s);
+    // gather + align + re-normalise: straight into the tensor-core Gram's transposed
+    // operand when it is used (m <= 1024), else into the row-major segment buffer
+    const bool tc_gram = gram_tc_supported(m, a.precision);
+    const bool fused = tc_gram && gather_transposed_supported(m);
+    const float* lead = nullptr;
+    if (fused) {
+        const GramOperand op = gram_tc_operand(ctx, n, k, m, a.precision);
+        float* first = ws.first.as<float>((size_t)k * m);
+        launch_gather_norm_t(a.x, perm, a.labels, shift, gate, offsets, counts, k, poff, n, m, op.fmt == 1, op.YT,
+                             op.YTlo, op.Pp, first, s);
+        lead = first;
+    } else {
+        seg = ws.seg.as<float>((size_t)std::max<int64_t>(n, 1) * m);
+        launch_gather_norm(a.x, perm, a.labels, shift, gate, n, m, seg, ctx->sm_count, s);
+        lead = seg;
+    }
 
     // Gram (padding columns b in [m, ld) stay zero)
     if (ld != m) TC_CUDA(cudaMemsetAsync(S, 0, sizeof(float) * (size_t)k * m * ld, s));
     TC_CUDA(cudaMemsetAsync(gram_err, 0, sizeof(int), s));
     const int nt = ceil_div(m, 64);
-    if (gram_tc_supported(m, a.precision)) {
-        launch_gram_tc(ctx, seg, counts, offsets, poff, n, k, m, ld, a.precision, S, gram_err, s);
+    if (tc_gram) {
+        launch_gram_tc(ctx, fused ? nullptr : seg, counts, offsets, poff, n, k, m, ld, a.precision, S, gram_err, s);
     } else {
         dim3 g(nt * (nt + 1) / 2, k);
         k_gram_simt<<<g, 256, 0, s>>>(seg, counts, offsets, m, ld, nt, S);
@@ -376,7 +393,7 @@ void extract_async(tc_ctx* ctx, const ExtractArgs& a, cudaStream_t s) {
     const bool full = a.cal_select || a.mode == TC_MODE_CANONICAL;
     const int tmax = full ? std::max(4 * m, 200) : m;
     const double tol = full ? 5e-7 : 1e-6;
-    power_eigvecs(ctx, S, ld, rs, tot, counts, offsets, seg, k, m, a.mode, tmax, tol, a.C, s);
+    power_eigvecs(ctx, S, ld, rs, tot, counts, offsets, lead, fused, k, m, a.mode, tmax, tol, a.C, s);
 }
 
 int run_extract(tc_ctx* ctx, const ExtractArgs& a, cudaStream_t s) {

@@ -41,7 +41,8 @@ struct PowerClusterParams {
     const double* tot;
     const int32_t* counts;
     const int32_t* offsets;
-    const float* seg;
+    const float* seg;  // members in cluster order, or (lead_rows) the first member of each cluster
+    int lead_rows;
     float* C;
     int k, m, tmax, mode;
     double tol2;
@@ -262,7 +263,7 @@ __global__ void __launch_bounds__(PC_THREADS, 1) k_power_cluster(PowerClusterPar
     // v = v_T (unit), y = u_{T+1} = M v_T in ybuf[T&1]
     if (rank == 0) {
         const float* y = ybuf + (T & 1) * ld;
-        const float* am = p.seg + (size_t)p.offsets[c] * m;
+        const float* am = p.seg + (size_t)(p.lead_rows ? c : p.offsets[c]) * m;
         double lam = 0;
         for (int a = threadIdx.x; a < m; a += PC_THREADS) lam += (double)v[a] * (double)y[a];
 #pragma unroll
@@ -351,10 +352,12 @@ static size_t cluster_smem(int m, int ld) {
 }
 
 void power_eigvecs(tc_ctx* ctx, const float* S, int ld, const double* r, const double* tot, const int32_t* counts,
-                   const int32_t* offsets, const float* seg, int k, int m, int mode, int tmax, double tol, float* C,
+                   const int32_t* offsets, const float* seg, bool lead_rows, int k, int m, int mode, int tmax,
+                   double tol, float* C,
                    cudaStream_t s) {
     int* steps = ctx->ws.pstats.as<int>((size_t)k);
-    PowerClusterParams pp{S, ld, r, tot, counts, offsets, seg, C, k, m, tmax, mode, tol * tol, steps};
+    PowerClusterParams pp{S, ld, r, tot, counts, offsets, seg, lead_rows ? 1 : 0, C, k, m, tmax, mode, tol * tol,
+                          steps};
     // long series stream tens of MB per step from HBM: spread each over 16 SMs
     if (m > 1024) {
         const size_t smem = cluster_smem<16>(m, ld);

@@ -126,6 +126,7 @@ struct Workspace {
     DevBuf gram;         // k*m*m f32
     DevBuf gram_yt;      // transposed, cluster-padded members for the tensor-core Gram
     DevBuf gram_poff;    // padded cluster offsets (int64)
+    DevBuf first;        // k*m f32: first aligned member of each cluster (fused gather)
     DevBuf rowsum;       // k*m f64 + k f64
     DevBuf piter;        // power-iteration vectors 3*k*m f32
     DevBuf pstats;       // 3*k*4 f64
@@ -204,6 +205,22 @@ struct ExtractArgs {
 void extract_async(tc_ctx* ctx, const ExtractArgs& a, cudaStream_t s);
 // extract_async, then reads and checks the flags; returns sum_class
 int run_extract(tc_ctx* ctx, const ExtractArgs& a, cudaStream_t s);
+
+// operand of the tensor-core Gram (transposed, cluster-padded members)
+struct GramOperand {
+    void* YT = nullptr;
+    float* YTlo = nullptr;  // 3xTF32 lo plane
+    int64_t Pp = 0;         // columns (padded positions)
+    int fmt = 0;            // 1 BF16, 2 TF32, 3 3xTF32
+};
+GramOperand gram_tc_operand(tc_ctx* ctx, int64_t n, int k, int m, int precision);
+// the extraction's gather written straight into that operand (m <= 1024), plus the
+// first member row of every cluster into first[k][m]
+bool gather_transposed_supported(int m);
+void launch_gather_norm_t(const float* x, const int32_t* perm, const int32_t* labels, const int32_t* shift,
+                          const uint8_t* gate, const int32_t* offsets, const int32_t* counts, int k,
+                          const int64_t* poff, int64_t n, int m, bool bf16, void* YT, float* YTlo, int64_t Pp,
+                          float* first, cudaStream_t s);
 
 // workspace of a context: free every buffer (the context must be idle) / bytes held
 void release_workspace(tc_ctx* ctx);

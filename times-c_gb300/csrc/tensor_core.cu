@@ -275,17 +275,31 @@ int64_t gram_padded_cols(int64_t n, int k) {
     return std::max<int64_t>((n + 63 * (int64_t)k + GT_PAD - 1) / GT_PAD * GT_PAD, GT_PAD);
 }
 
+// The transposed, cluster-padded operand of the tensor-core Gram in the workspace:
+// BF16 (precision BF16), TF32 (TF32), or TF32 hi and lo planes (FP32: 3xTF32).
+GramOperand gram_tc_operand(tc_ctx* ctx, int64_t n, int k, int m, int precision) {
+    GramOperand o;
+    o.Pp = gram_padded_cols(n, k);
+    o.fmt = precision == TC_PREC_BF16 ? 1 : (precision == TC_PREC_TF32 ? 2 : 3);
+    const int esize = o.fmt == 1 ? 2 : 4;
+    const size_t plane = (size_t)m * o.Pp * esize;
+    char* YT = static_cast<char*>(ctx->ws.gram_yt.get(plane * (o.fmt == 3 ? 2 : 1)));
+    o.YT = YT;
+    o.YTlo = o.fmt == 3 ? reinterpret_cast<float*>(YT + plane) : nullptr;
+    return o;
+}
+
 // No host synchronisation: a pipeline wait that runs out sets *err (the caller reads it).
+// seg == nullptr: the operand was already written by the fused gather.
 void launch_gram_tc(tc_ctx* ctx, const float* seg, const int32_t* counts, const int32_t* offsets,
                     const int64_t* poff, int64_t n, int k, int m, int ld, int precision, float* S, int* err,
                     cudaStream_t s) {
-    Workspace& ws = ctx->ws;
-    const int64_t Pp = gram_padded_cols(n, k);
-    const int fmt = precision == TC_PREC_BF16 ? 1 : (precision == TC_PREC_TF32 ? 2 : 3);
+    const GramOperand op = gram_tc_operand(ctx, n, k, m, precision);
+    const int64_t Pp = op.Pp;
+    const int fmt = op.fmt;
     const int esize = fmt == 1 ? 2 : 4;
-    const size_t plane = (size_t)m * Pp * esize;
-    char* YT = static_cast<char*>(ws.gram_yt.get(plane * (fmt == 3 ? 2 : 1)));
-    float* YTlo = fmt == 3 ? reinterpret_cast<float*>(YT + plane) : nullptr;
+    char* YT = static_cast<char*>(op.YT);
+    float* YTlo = op.YTlo;
     // only the padding needs zeros: the transpose writes every member column
     if (fmt == 1)
         k_zero_pads<__nv_bfloat16><<<k, 256, 0, s>>>(counts, poff, m, Pp, (__nv_bfloat16*)YT, nullptr);
@@ -293,7 +307,7 @@ void launch_gram_tc(tc_ctx* ctx, const float* seg, const int32_t* counts, const 
         k_zero_pads<float><<<k, 256, 0, s>>>(counts, poff, m, Pp, (float*)YT, YTlo);
     TC_CHECK_LAUNCH();
     dim3 tg(ceil_div(n, 32), ceil_div(m, 32)), tb(32, 8);
-    if (n > 0) {
+    if (n > 0 && seg) {
         if (fmt == 1)
             k_seg_transpose<__nv_bfloat16><<<tg, tb, 0, s>>>(seg, n, m, offsets, counts, poff, k,
                                                              (__nv_bfloat16*)YT, nullptr, Pp);

@@ -8,6 +8,8 @@
 // shifted by its alignment shift (out[t] = x[t - shift], zero fill, SBD.cuh:14-29)
 // and writes the normalised row to position pos of the cluster-ordered buffer
 // (block_alloc2D + sbd3D + z_norm_gpu_x of shapeExtract.cuh:1117-1141).
+#include <cuda_bf16.h>
+
 #include "tc_internal.h"
 
 namespace tc {
@@ -24,11 +26,14 @@ struct RowSrc {
 };
 
 template <bool GATHER>
-__device__ __forceinline__ RowSrc row_source(const float* src, int64_t row, int m, const int32_t* perm,
+__device__ __forceinline__ RowSrc row_source(const float* src, int64_t row, int64_t n, int m, const int32_t* perm,
                                              const int32_t* labels, const int32_t* shift, const uint8_t* gate) {
     RowSrc r;
     if (GATHER) {
         int64_t i = perm[row];
+        // an entry the scatter did not fill (labels outside [0, k), reported as an
+        // error by the host) reads row 0 instead of an arbitrary address
+        if (i < 0 || i >= n) i = 0;
         r.x = src + (size_t)i * m;
         r.shift = (gate && shift && gate[labels[i]]) ? shift[i] : 0;
     } else {
@@ -72,7 +77,7 @@ __global__ void __launch_bounds__(256) k_norm_rows_warp(const float* __restrict_
     const int64_t w0 = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
     for (int64_t row = w0; row < n; row += nw) {
-        RowSrc rs = row_source<GATHER>(src, row, m, perm, labels, shift, gate);
+        RowSrc rs = row_source<GATHER>(src, row, n, m, perm, labels, shift, gate);
         float v[VPL];
         KSum s;
 #pragma unroll
@@ -112,7 +117,7 @@ __global__ void __launch_bounds__(256) k_norm_rows_block(const float* __restrict
     __shared__ double red[8];
     const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
     for (int64_t row = blockIdx.x; row < n; row += gridDim.x) {
-        RowSrc rs = row_source<GATHER>(src, row, m, perm, labels, shift, gate);
+        RowSrc rs = row_source<GATHER>(src, row, n, m, perm, labels, shift, gate);
         float v[VPT];
         float s = 0.f;
 #pragma unroll
@@ -186,6 +191,133 @@ void launch_znorm(float* x, int64_t n, int m, int ddof, int sm_count, cudaStream
 void launch_gather_norm(const float* x, const int32_t* perm, const int32_t* labels, const int32_t* shift,
                         const uint8_t* gate, int64_t n, int m, float* seg, int sm_count, cudaStream_t s) {
     norm_rows<true>(x, seg, n, m, 1, perm, labels, shift, gate, sm_count, s);
+}
+
+}  // namespace tc
+
+// ---------------------------------------------------------------- fused gather + transpose
+namespace tc {
+
+template <class TO>
+__device__ __forceinline__ TO to_operand(float v);
+template <>
+__device__ __forceinline__ __nv_bfloat16 to_operand<__nv_bfloat16>(float v) { return __float2bfloat16_rn(v); }
+template <>
+__device__ __forceinline__ float to_operand<float>(float v) {  // TF32 rounding (the 3xTF32 hi part)
+    uint32_t r;
+    asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(r) : "f"(v));
+    return __uint_as_float(r);
+}
+
+// The extraction's gather (align + re-normalise, as k_norm_rows_warp<VPL, true>,
+// with the same arithmetic) for 32 cluster-ordered positions per block, written
+// transposed into the tensor-core Gram's operand YT[a][pp] (pp: the position in
+// the cluster-padded layout) instead of row-major: the row-major copy and the
+// separate transpose pass are never made.  The first member of each cluster also
+// goes to first[c][*] (the sign rule's reference row).  With YTlo (3xTF32) the lo
+// plane gets x - tf32(x) rounded to TF32.  Rows are staged in shared memory with
+// pitch m+1 so the transposed reads are free of bank conflicts.
+template <int VPL, class TO>
+__global__ void __launch_bounds__(256) k_gather_norm_t(const float* __restrict__ src, int64_t n, int m,
+                                                       const int32_t* __restrict__ perm,
+                                                       const int32_t* __restrict__ labels,
+                                                       const int32_t* __restrict__ shift,
+                                                       const uint8_t* __restrict__ gate,
+                                                       const int32_t* __restrict__ offsets,
+                                                       const int32_t* __restrict__ counts, int k,
+                                                       const int64_t* __restrict__ poff, TO* __restrict__ YT,
+                                                       float* __restrict__ YTlo, int64_t Pp,
+                                                       float* __restrict__ first) {
+    extern __shared__ float tile[];  // [32][m + 1]
+    const int pitch = m + 1;
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    const int64_t pos0 = (int64_t)blockIdx.x * 32;
+    // positions the scatter filled (fewer than n when some labels were outside [0, k):
+    // the host reports that as an error, and nothing here reads the unfilled ones)
+    const int64_t placed = (int64_t)offsets[k - 1] + counts[k - 1];
+    for (int r = wid; r < 32; r += 8) {
+        const int64_t pos = pos0 + r;
+        if (pos >= placed) break;
+        const int64_t i = perm[pos];
+        const int c = labels[i];
+        const float* x = src + (size_t)i * m;
+        const int sh = (gate && shift && gate[c]) ? shift[i] : 0;
+        float v[VPL];
+        KSum s;
+#pragma unroll
+        for (int q = 0; q < VPL; ++q) {
+            const int t = lane + 32 * q, a = t - sh;
+            v[q] = (t < m && a >= 0 && a < m) ? x[a] : 0.f;
+            s.add(v[q]);
+        }
+        const float mean = warp_sum_comp(s) / (float)m;
+        KSum ss;
+#pragma unroll
+        for (int q = 0; q < VPL; ++q) {
+            const int t = lane + 32 * q;
+            const float d = t < m ? v[q] - mean : 0.f;
+            v[q] = d;
+            ss.add(d * d);
+        }
+        const float var = warp_sum_comp(ss) / (float)(m - 1);
+        const float sd = sqrtf(var);
+        const float inv = (sd > 0.f && isfinite(sd)) ? 1.0f / sd : 0.f;
+        const bool lead = pos == offsets[c];
+#pragma unroll
+        for (int q = 0; q < VPL; ++q) {
+            const int t = lane + 32 * q;
+            if (t < m) {
+                const float y = v[q] * inv;
+                tile[r * pitch + t] = y;
+                if (lead) first[(size_t)c * m + t] = y;
+            }
+        }
+    }
+    __syncthreads();
+    const int r = lane;
+    const int64_t pos = pos0 + r;
+    if (pos >= placed) return;
+    const int c = labels[perm[pos]];
+    const int64_t pp = pos - offsets[c] + poff[c];
+    for (int a = wid; a < m; a += 8) {
+        const float y = tile[r * pitch + a];
+        const TO hi = to_operand<TO>(y);
+        YT[(int64_t)a * Pp + pp] = hi;
+        if (YTlo) YTlo[(int64_t)a * Pp + pp] = to_operand<float>(y - (float)hi);
+    }
+}
+
+bool gather_transposed_supported(int m) { return m >= 2 && m <= 1024; }
+
+void launch_gather_norm_t(const float* x, const int32_t* perm, const int32_t* labels, const int32_t* shift,
+                          const uint8_t* gate, const int32_t* offsets, const int32_t* counts, int k,
+                          const int64_t* poff, int64_t n, int m, bool bf16, void* YT, float* YTlo, int64_t Pp,
+                          float* first, cudaStream_t s) {
+    if (n == 0) return;
+    TC_REQUIRE(gather_transposed_supported(m), TC_ERR_UNSUPPORTED, "fused gather: m must be in [2, 1024]");
+    const size_t smem = (size_t)32 * (m + 1) * sizeof(float);
+    const int grid = ceil_div(n, 32);
+#define GT(VPL)                                                                                                 \
+    do {                                                                                                        \
+        if (bf16) {                                                                                             \
+            allow_max_dynamic_smem(k_gather_norm_t<VPL, __nv_bfloat16>);                                        \
+            k_gather_norm_t<VPL, __nv_bfloat16><<<grid, 256, smem, s>>>(x, n, m, perm, labels, shift, gate,     \
+                                                                        offsets, counts, k, poff,               \
+                                                                        (__nv_bfloat16*)YT,                     \
+                                                                        nullptr, Pp, first);                   \
+        } else {                                                                                                \
+            allow_max_dynamic_smem(k_gather_norm_t<VPL, float>);                                                \
+            k_gather_norm_t<VPL, float><<<grid, 256, smem, s>>>(x, n, m, perm, labels, shift, gate, offsets,    \
+                                                                counts, k, poff, (float*)YT, YTlo, Pp, first);  \
+        }                                                                                                       \
+    } while (0)
+    if (m <= 64) GT(2);
+    else if (m <= 128) GT(4);
+    else if (m <= 256) GT(8);
+    else if (m <= 512) GT(16);
+    else GT(32);
+#undef GT
+    TC_CHECK_LAUNCH();
 }
 
 }  // namespace tc
