@@ -79,15 +79,17 @@ __global__ void __launch_bounds__(PC_THREADS, 1) k_power_cluster(PowerClusterPar
     if (p.counts[c] == 0) return;  // every CTA of this cluster leaves together
     const int a0 = (int)((int64_t)rank * m / CL), a1 = (int)((int64_t)(rank + 1) * m / CL);
     const int nrow = a1 - a0;
-    // shared memory: v[ld] | y[2][ld] | part[2][CL][4] doubles | vprev[nrow] | r_own[nrow]
+    // shared memory: v[ld] | y[2][ld] | part[2][CL][warps][4] float pairs | vprev[nrow] | r_own[nrow]
     auto a16 = [](size_t x) { return (x + 15) & ~size_t(15); };
     float* v = reinterpret_cast<float*>(dsm);
     float* ybuf = reinterpret_cast<float*>(dsm + a16((size_t)ld * 4));
+    constexpr int NWARP = PC_THREADS / 32;
+    // per-step partial sums of every warp of every CTA: part[parity][rank][warp][4]
     float2* part = reinterpret_cast<float2*>(dsm + a16((size_t)ld * 4) + a16((size_t)2 * ld * 4));
-    float* vprev = reinterpret_cast<float*>(reinterpret_cast<unsigned char*>(part) + a16((size_t)2 * CL * 4 * 8));
+    float* vprev = reinterpret_cast<float*>(reinterpret_cast<unsigned char*>(part) +
+                                            a16((size_t)2 * CL * NWARP * 4 * 8));
     float* r_own = vprev + a16((size_t)nrow * 4) / 4;
     __shared__ double red[PC_THREADS / 32][4];
-    __shared__ float2 red2[PC_THREADS / 32][4];  // per-step partials
     __shared__ float sh_corr[2];
     __shared__ double sh_inv;
     __shared__ int sh_done;
@@ -137,12 +139,14 @@ __global__ void __launch_bounds__(PC_THREADS, 1) k_power_cluster(PowerClusterPar
     }
     cluster.sync();  // every CTA initialised before remote stores start
     int T = p.tmax;
-    const float4* v4 = reinterpret_cast<const float4*>(v);
     const int nv4 = ld / 4;
     constexpr int U = BPL >= 8 ? 2 : PC_UNROLL;  // rows in flight per warp
+    float fsc = 1.f;  // v_t = ybuf[(t-1)&1] * fsc for t >= 1 (the FP32 product the update stored before)
     for (int t = 0;; ++t) {
         const int par = t & 1;
         const float cr = sh_corr[0], cc = sh_corr[1];
+        const float* vt = t == 0 ? v : ybuf + (par ^ 1) * ld;  // u_t, scaled by fsc below
+        const float4* vt4 = reinterpret_cast<const float4*>(vt);
         // per-step sums as FP32 pairs (value = s - c), exact products by FMA: GB300's
         // FP64 pipe is too narrow for per-row double arithmetic
         float accs[4] = {0.f, 0.f, 0.f, 0.f}, accc[4] = {0.f, 0.f, 0.f, 0.f};
@@ -182,14 +186,22 @@ __global__ void __launch_bounds__(PC_THREADS, 1) k_power_cluster(PowerClusterPar
                 for (int j = 0; j < BPL; ++j) {
                     const int b = lane + 32 * j;
                     if (b < nv4) {
-                        const float4 w = v4[b];
+                        float4 w = vt4[b];
+                        w.x *= fsc;
+                        w.y *= fsc;
+                        w.z *= fsc;
+                        w.w *= fsc;
 #pragma unroll
                         for (int u = 0; u < U; ++u) kahan4(u, x[u][j], w);
                     }
                 }
             } else {
                 for (int b = lane; b < nv4; b += 32) {
-                    const float4 w = v4[b];
+                    float4 w = vt4[b];
+                    w.x *= fsc;
+                    w.y *= fsc;
+                    w.z *= fsc;
+                    w.w *= fsc;
                     float4 x[U];
 #pragma unroll
                     for (int u = 0; u < U; ++u) x[u] = __ldg(rowp[u] + b);
@@ -215,7 +227,7 @@ __global__ void __launch_bounds__(PC_THREADS, 1) k_power_cluster(PowerClusterPar
                         add_prod(0, yf, yf);
                         two_sum_acc(accs[1], accc[1], yf, 0.f);
                         add_prod(2, ra, yf);
-                        const float va = v[a];
+                        const float va = vt[a] * fsc;
                         if (t >= 1) {
                             const float d = va - vprev[i];
                             add_prod(3, d, d);
@@ -225,39 +237,53 @@ __global__ void __launch_bounds__(PC_THREADS, 1) k_power_cluster(PowerClusterPar
                 }
             }
         }
-        if (lane == 0)
-            for (int q = 0; q < 4; ++q) red2[wid][q] = make_float2(accs[q], accc[q]);
-        __syncthreads();
-        if (threadIdx.x < 4) {
-            float ss = 0.f, sc = 0.f;
-            for (int w = 0; w < nw; ++w) two_sum_acc(ss, sc, red2[w][threadIdx.x].x, red2[w][threadIdx.x].y);
+        // every warp's partial (held by lane 0) straight into every CTA, lane q storing into
+        // CTA q: no CTA barrier before the exchange
+        float2 mine[4];
 #pragma unroll
-            for (int q = 0; q < CL; ++q) prem[q][(par * CL + rank) * 4 + threadIdx.x] = make_float2(ss, sc);
+        for (int q = 0; q < 4; ++q)
+            mine[q] = make_float2(__shfl_sync(0xffffffffu, accs[q], 0), __shfl_sync(0xffffffffu, accc[q], 0));
+        if (lane < CL) {
+            float2* dst = prem[lane] + ((size_t)(par * CL + rank) * NWARP + wid) * 4;
+#pragma unroll
+            for (int q = 0; q < 4; ++q) dst[q] = mine[q];
         }
         cluster.sync();  // y and partials of step t visible in every CTA
-        if (threadIdx.x == 0) {  // identical in every CTA (rank order)
+        if (wid == 0) {  // the same fixed order in every CTA, so all take the same decision
             float ts[4] = {0.f, 0.f, 0.f, 0.f}, tcm[4] = {0.f, 0.f, 0.f, 0.f};
-            for (int q = 0; q < CL; ++q) {
-                const float2* pq = part + (par * CL + q) * 4;
+            const float2* pp = part + (size_t)par * CL * NWARP * 4;
+            for (int e = lane; e < CL * NWARP; e += 32)
 #pragma unroll
-                for (int e = 0; e < 4; ++e) two_sum_acc(ts[e], tcm[e], pq[e].x, pq[e].y);
+                for (int q = 0; q < 4; ++q) two_sum_acc(ts[q], tcm[q], pp[e * 4 + q].x, pp[e * 4 + q].y);
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1)
+#pragma unroll
+                for (int q = 0; q < 4; ++q) {
+                    const float s2 = __shfl_xor_sync(0xffffffffu, ts[q], o);
+                    const float c2 = __shfl_xor_sync(0xffffffffu, tcm[q], o);
+                    two_sum_acc(ts[q], tcm[q], s2, c2);
+                }
+            if (lane == 0) {
+                const double n2 = (double)ts[0] - (double)tcm[0], sy = (double)ts[1] - (double)tcm[1];
+                const double ry = (double)ts[2] - (double)tcm[2], dd = (double)ts[3] - (double)tcm[3];
+                const double inv = rsqrt_d(n2), sv = sy * inv, rv = ry * inv;
+                sh_corr[0] = (float)(-sv * inv_m);
+                sh_corr[1] = (float)(-rv * inv_m + totc * sv * inv_m * inv_m);
+                sh_inv = inv;
+                sh_done = t >= p.tmax || (t >= 1 && dd < p.tol2) || !(n2 > 0);
             }
-            const double n2 = (double)ts[0] - (double)tcm[0], sy = (double)ts[1] - (double)tcm[1];
-            const double ry = (double)ts[2] - (double)tcm[2], dd = (double)ts[3] - (double)tcm[3];
-            const double inv = rsqrt_d(n2), sv = sy * inv, rv = ry * inv;
-            sh_corr[0] = (float)(-sv * inv_m);
-            sh_corr[1] = (float)(-rv * inv_m + totc * sv * inv_m * inv_m);
-            sh_inv = inv;
-            sh_done = t >= p.tmax || (t >= 1 && dd < p.tol2) || !(n2 > 0);
         }
         __syncthreads();
         if (sh_done) {
             T = t;
             break;
         }
-        const float finv = (float)sh_inv;
-        const float* y = ybuf + par * ld;
-        for (int a = threadIdx.x; a < m; a += PC_THREADS) v[a] = y[a] * finv;
+        fsc = (float)sh_inv;  // v_{t+1} = u_{t+1} * fsc, read from ybuf[par] in the next step
+    }
+    if (T >= 1) {  // materialise v_T = ybuf[(T-1)&1] * (its scale) for the final step
+        const float* yv = ybuf + ((T - 1) & 1) * ld;
+        __syncthreads();
+        for (int a = threadIdx.x; a < m; a += PC_THREADS) v[a] = yv[a] * fsc;
         __syncthreads();
     }
     // v = v_T (unit), y = u_{T+1} = M v_T in ybuf[T&1]
@@ -347,7 +373,8 @@ template <int CL>
 static size_t cluster_smem(int m, int ld) {
     auto a16 = [](size_t x) { return (x + 15) & ~size_t(15); };
     const int nrow = (m + CL - 1) / CL;
-    return a16((size_t)ld * 4) + a16((size_t)2 * ld * 4) + a16((size_t)2 * CL * 4 * 8) + a16((size_t)nrow * 4) +
+    constexpr int NWARP = PC_THREADS / 32;
+    return a16((size_t)ld * 4) + a16((size_t)2 * ld * 4) + a16((size_t)2 * CL * NWARP * 4 * 8) + a16((size_t)nrow * 4) +
            (size_t)nrow * 4;
 }
 
