@@ -25,11 +25,6 @@ namespace tc {
 
 void launch_gather_norm(const float* x, const int32_t* perm, const int32_t* labels, const int32_t* shift,
                         const uint8_t* gate, int64_t n, int m, float* seg, int sm_count, cudaStream_t s);
-bool gram_tc_supported(int m, int precision);
-void launch_gram_tc(tc_ctx* ctx, const float* seg, const int32_t* counts, const int32_t* offsets,
-                    const int64_t* poff, int64_t n, int k, int m, int ld, int precision, float* S, int* err,
-                    cudaStream_t s);
-int64_t gram_padded_cols(int64_t n, int k);
 
 constexpr int SEG_CHUNK = 4096;
 constexpr int SEG_BLOCK = 256;
@@ -284,8 +279,7 @@ __global__ void k_rowsum_total(const double* __restrict__ r, const int32_t* __re
 
 void power_eigvecs(tc_ctx* ctx, const float* S, int ld, const double* r, const double* tot, const int32_t* counts,
                    const int32_t* offsets, const float* seg, bool lead_rows, int k, int m, int mode, int tmax,
-                   double tol, float* C,
-                   cudaStream_t s);
+                   double tol, const float* vinit, const int32_t* vok, int tmax_sq, float* C, cudaStream_t s);
 
 // ---------------------------------------------------------------- driver
 // Everything on the stream, with no host synchronisation (capturable in a CUDA
@@ -358,6 +352,10 @@ void extract_async(tc_ctx* ctx, const ExtractArgs& a, cudaStream_t s) {
     // operand when it is used (m <= 1024), else into the row-major segment buffer
     const bool tc_gram = gram_tc_supported(m, a.precision);
     const bool fused = tc_gram && gather_transposed_supported(m);
+    const bool squaring =
+        (a.cal_select || a.mode == TC_MODE_CANONICAL) && power_squaring_supported(m, k, ctx->sm_count);
+    if (tc_gram && squaring)  // one operand buffer for both uses, sized before either is written
+        ws.gram_yt.get(std::max(gram_operand_bytes(n, k, m, a.precision), power_squaring_operand_bytes(k, m)));
     const float* lead = nullptr;
     if (fused) {
         const GramOperand op = gram_tc_operand(ctx, n, k, m, a.precision);
@@ -393,7 +391,22 @@ void extract_async(tc_ctx* ctx, const ExtractArgs& a, cudaStream_t s) {
     const bool full = a.cal_select || a.mode == TC_MODE_CANONICAL;
     const int tmax = full ? std::max(4 * m, 200) : m;
     const double tol = full ? 5e-7 : 1e-6;
-    power_eigvecs(ctx, S, ld, rs, tot, counts, offsets, lead, fused, k, m, a.mode, tmax, tol, a.C, s);
+    // The converging forms start from M^e v_0, e = 2^J >= tmax, by repeated squaring on
+    // the tensor cores, and step on until the convergence test passes.  The compat form
+    // keeps its m plain steps: an error eps in the j-th square is applied m/2^j times, so
+    // with FP32 accumulation (eps ~ 1e-6) a cluster whose top two eigenvalues nearly tie
+    // would drift by ~m*eps from the m-step vector, which the steps themselves hold to
+    // ~1e-7 per step.
+    SquaringResult sq;
+    int tmax_sq = 0;
+    if (squaring) {
+        int64_t e = 1;
+        while (e < tmax) e <<= 1;
+        tmax_sq = tmax;
+        sq = power_squaring(ctx, S, ld, rs, tot, counts, k, m, e, gram_err, s);
+    }
+    power_eigvecs(ctx, S, ld, rs, tot, counts, offsets, lead, fused, k, m, a.mode, tmax, tol, sq.vec, sq.ok, tmax_sq,
+                  a.C, s);
 }
 
 int run_extract(tc_ctx* ctx, const ExtractArgs& a, cudaStream_t s) {

@@ -176,12 +176,14 @@ uint64_t tc_job_footprint(const tc_job* j) {
     b += n * m * 4;                        // members in cluster order
     b += n * 4 * 5;                        // labels, old labels, shifts, distances, permutation
     b += k * m * 4 + k * (F / 2 + 1) * 8;  // centroids, spectra
-    b += k * m * ld * 4;                   // Gram matrices
+    b += 2 * k * m * ld * 4;               // Gram matrices and their squares (power by squaring)
     b += (k * m + k) * 8 + 3 * k * m * 4;  // row sums, power-iteration vectors
     b += k * 8 * 4;                        // counts, offsets, padded offsets, gates
     const uint64_t esize = j->precision == TC_PREC_BF16 ? 2 : 4;
     const uint64_t planes = j->precision == TC_PREC_FP32 ? 2 : 1;
-    b += m * Pp * esize * planes;          // transposed members for the tensor-core Gram
+    const uint64_t mp64 = (m + 63) / 64 * 64;
+    const uint64_t Psq = std::max<uint64_t>((k * mp64 + 63 * k + 63) / 64 * 64, 64);
+    b += std::max(m * Pp * esize * planes, m * Psq * 8);  // Gram operand (members, or the squared matrices)
     if (j->precision != TC_PREC_FP32 && tc::tc_assign_supported(j->m, (int)F, j->k, j->precision)) {
         const uint64_t mp = (m + 63) / 64 * 64;
         b += n * mp * 2 + n * 4;           // BF16 series and norms

@@ -3,7 +3,9 @@
 // of get_center, :217-264).
 //
 // M v = S v - (1.v/m) r - (r.v/m) 1 + (tot 1.v/m^2) 1 with r = S 1 and tot = 1^T S 1,
-// so M is never formed.  Step t: v_t = u_t/|u_t|, u_{t+1} = M v_t.
+// so M is never formed.  Step t: v_t = u_t/|u_t|, u_{t+1} = M v_t.  Where the
+// repeated squaring (power_sq.cu) produced M^e v_0, the iteration starts from that
+// vector instead, with its own step cap.
 //
 // One thread-block cluster of CL CTAs per k-Shape cluster c.  CTA `rank` owns rows
 // [rank*m/CL, (rank+1)*m/CL) of S_c and streams them (float4, row pitch ld) from
@@ -47,6 +49,11 @@ struct PowerClusterParams {
     int k, m, tmax, mode;
     double tol2;
     int* steps;  // per cluster: the step T whose vector was stored (diagnostics)
+    // start vectors from the repeated squaring (k x ld, any scale) where vok[c];
+    // such clusters run at most tmax_sq steps
+    const float* vinit;
+    const int32_t* vok;
+    int tmax_sq;
 };
 
 // (s, c) += (s2, c2) where a pair means s - c; the two leading parts are added
@@ -99,11 +106,14 @@ __global__ void __launch_bounds__(PC_THREADS, 1) k_power_cluster(PowerClusterPar
     const double inv_m = 1.0 / (double)m, totc = p.tot[c];
     for (int i = threadIdx.x; i < nrow; i += PC_THREADS) r_own[i] = (float)rc[a0 + i];
 
-    // v_0 = [1, .5, 1, .5, ...] / |.|, with its sum and r.v (identical in every CTA)
+    // v_0 = [1, .5, 1, .5, ...] / |.| (or the squaring's vector, normalised), with its
+    // sum and r.v (identical in every CTA)
+    const float* vi = (p.vinit && p.vok[c]) ? p.vinit + (size_t)c * ld : nullptr;
+    int tmax = p.tmax;
     {
         double s2 = 0, s1 = 0, sr = 0;
         for (int a = threadIdx.x; a < m; a += PC_THREADS) {
-            const double x = (a % 2 == 0) ? 1.0 : 0.5;
+            const double x = vi ? (double)vi[a] : ((a % 2 == 0) ? 1.0 : 0.5);
             s2 += x * x;
             s1 += x;
             sr += rc[a] * x;
@@ -119,14 +129,30 @@ __global__ void __launch_bounds__(PC_THREADS, 1) k_power_cluster(PowerClusterPar
         if (threadIdx.x == 0) {
             double t2 = 0, t1 = 0, tr = 0;
             for (int w = 0; w < nw; ++w) { t2 += red[w][0]; t1 += red[w][1]; tr += red[w][2]; }
+            const bool use = vi && t2 > 0 && t2 < 1e300;  // a zero or non-finite product: start from v0
+            if (vi && !use) {
+                t2 = 0;
+                t1 = 0;
+                tr = 0;
+                for (int a = 0; a < m; ++a) {
+                    const double x = (a % 2 == 0) ? 1.0 : 0.5;
+                    t2 += x * x;
+                    t1 += x;
+                    tr += rc[a] * x;
+                }
+            }
             const double inv = rsqrt_d(t2), sv = t1 * inv, rv = tr * inv;
             sh_corr[0] = (float)(-sv * inv_m);
             sh_corr[1] = (float)(-rv * inv_m + totc * sv * inv_m * inv_m);
             sh_inv = inv;
+            sh_done = use;
         }
         __syncthreads();
         const float finv = (float)sh_inv;
-        for (int a = threadIdx.x; a < ld; a += PC_THREADS) v[a] = a < m ? ((a % 2 == 0) ? 1.0f : 0.5f) * finv : 0.f;
+        if (!sh_done) vi = nullptr;
+        else tmax = p.tmax_sq;
+        for (int a = threadIdx.x; a < ld; a += PC_THREADS)
+            v[a] = a < m ? (vi ? vi[a] : ((a % 2 == 0) ? 1.0f : 0.5f)) * finv : 0.f;
         for (int a = threadIdx.x; a < 2 * ld; a += PC_THREADS) ybuf[a] = 0.f;  // padding stays zero
         __syncthreads();
     }
@@ -138,7 +164,7 @@ __global__ void __launch_bounds__(PC_THREADS, 1) k_power_cluster(PowerClusterPar
         prem[q] = cluster.map_shared_rank(part, q);
     }
     cluster.sync();  // every CTA initialised before remote stores start
-    int T = p.tmax;
+    int T = tmax;
     const int nv4 = ld / 4;
     constexpr int U = BPL >= 8 ? 2 : PC_UNROLL;  // rows in flight per warp
     float fsc = 1.f;  // v_t = ybuf[(t-1)&1] * fsc for t >= 1 (the FP32 product the update stored before)
@@ -270,7 +296,7 @@ __global__ void __launch_bounds__(PC_THREADS, 1) k_power_cluster(PowerClusterPar
                 sh_corr[0] = (float)(-sv * inv_m);
                 sh_corr[1] = (float)(-rv * inv_m + totc * sv * inv_m * inv_m);
                 sh_inv = inv;
-                sh_done = t >= p.tmax || (t >= 1 && dd < p.tol2) || !(n2 > 0);
+                sh_done = t >= tmax || (t >= 1 && dd < p.tol2) || !(n2 > 0);
             }
         }
         __syncthreads();
@@ -380,11 +406,10 @@ static size_t cluster_smem(int m, int ld) {
 
 void power_eigvecs(tc_ctx* ctx, const float* S, int ld, const double* r, const double* tot, const int32_t* counts,
                    const int32_t* offsets, const float* seg, bool lead_rows, int k, int m, int mode, int tmax,
-                   double tol, float* C,
-                   cudaStream_t s) {
+                   double tol, const float* vinit, const int32_t* vok, int tmax_sq, float* C, cudaStream_t s) {
     int* steps = ctx->ws.pstats.as<int>((size_t)k);
-    PowerClusterParams pp{S, ld, r, tot, counts, offsets, seg, lead_rows ? 1 : 0, C, k, m, tmax, mode, tol * tol,
-                          steps};
+    PowerClusterParams pp{S,  ld, r,  tot,        counts, offsets, seg,   lead_rows ? 1 : 0, C, k, m, tmax, mode,
+                          tol * tol, steps, vinit, vok, tmax_sq};
     // long series stream tens of MB per step from HBM: spread each over 16 SMs
     if (m > 1024) {
         const size_t smem = cluster_smem<16>(m, ld);

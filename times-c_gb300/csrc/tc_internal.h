@@ -128,7 +128,9 @@ struct Workspace {
     DevBuf gram_poff;    // padded cluster offsets (int64)
     DevBuf first;        // k*m f32: first aligned member of each cluster (fused gather)
     DevBuf rowsum;       // k*m f64 + k f64
-    DevBuf piter;        // power-iteration vectors 3*k*m f32
+    DevBuf piter;        // power-by-squaring vectors 2*k*ld f32
+    DevBuf gram_sq;      // k*m*ld f32: squares of the power-by-squaring matrices
+    DevBuf sq_meta;      // k int64 padded offsets + 2k int32 (column counts, flags)
     DevBuf pstats;       // 3*k*4 f64
     DevBuf aux;          // small scalars (changed count, dist sum, sum_class, flags)
     DevBuf toeplitz;     // bf16 shifted centroid copies for the tensor-core correlation
@@ -214,6 +216,22 @@ struct GramOperand {
     int fmt = 0;            // 1 BF16, 2 TF32, 3 3xTF32
 };
 GramOperand gram_tc_operand(tc_ctx* ctx, int64_t n, int k, int m, int precision);
+size_t gram_operand_bytes(int64_t n, int k, int m, int precision);
+bool gram_tc_supported(int m, int precision);
+int64_t gram_padded_cols(int64_t n, int k);
+// S_c = YT_c YT_c^T for every cluster (seg == nullptr: the operand is already in place)
+void launch_gram_tc(tc_ctx* ctx, const float* seg, const int32_t* counts, const int32_t* offsets,
+                    const int64_t* poff, int64_t n, int k, int m, int ld, int precision, float* S, int* err,
+                    cudaStream_t s);
+// power iteration by repeated squaring (power_sq.cu): vec[c] ~ M_c^e v0 where ok[c]
+struct SquaringResult {
+    const float* vec = nullptr;  // k x ld, not normalised
+    const int32_t* ok = nullptr;  // k flags
+};
+bool power_squaring_supported(int m, int k, int sm_count);
+size_t power_squaring_operand_bytes(int k, int m);
+SquaringResult power_squaring(tc_ctx* ctx, const float* S, int ld, const double* r, const double* tot,
+                              const int32_t* counts, int k, int m, int64_t e, int* err, cudaStream_t s);
 // the extraction's gather written straight into that operand (m <= 1024), plus the
 // first member row of every cluster into first[k][m]
 bool gather_transposed_supported(int m);

@@ -277,13 +277,18 @@ int64_t gram_padded_cols(int64_t n, int k) {
 
 // The transposed, cluster-padded operand of the tensor-core Gram in the workspace:
 // BF16 (precision BF16), TF32 (TF32), or TF32 hi and lo planes (FP32: 3xTF32).
+size_t gram_operand_bytes(int64_t n, int k, int m, int precision) {
+    const int fmt = precision == TC_PREC_BF16 ? 1 : (precision == TC_PREC_TF32 ? 2 : 3);
+    return (size_t)m * gram_padded_cols(n, k) * (fmt == 1 ? 2 : 4) * (fmt == 3 ? 2 : 1);
+}
+
 GramOperand gram_tc_operand(tc_ctx* ctx, int64_t n, int k, int m, int precision) {
     GramOperand o;
     o.Pp = gram_padded_cols(n, k);
     o.fmt = precision == TC_PREC_BF16 ? 1 : (precision == TC_PREC_TF32 ? 2 : 3);
     const int esize = o.fmt == 1 ? 2 : 4;
     const size_t plane = (size_t)m * o.Pp * esize;
-    char* YT = static_cast<char*>(ctx->ws.gram_yt.get(plane * (o.fmt == 3 ? 2 : 1)));
+    char* YT = static_cast<char*>(ctx->ws.gram_yt.get(gram_operand_bytes(n, k, m, precision)));
     o.YT = YT;
     o.YTlo = o.fmt == 3 ? reinterpret_cast<float*>(YT + plane) : nullptr;
     return o;
