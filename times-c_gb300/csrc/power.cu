@@ -75,7 +75,9 @@ __device__ __forceinline__ double rsqrt_d(double x) {
 }
 
 // BPL > 0: rows of at most 32*BPL float4 (loads unrolled); 0: any length.
-template <int CL, int BPL>
+// RES: the CTA's rows of S_c are copied into shared memory once and every step reads
+// them there (when they fit: m <= ~600 with 8 CTAs per cluster), else from L2.
+template <int CL, int BPL, bool RES>
 __global__ void __launch_bounds__(PC_THREADS, 1) k_power_cluster(PowerClusterParams p) {
     namespace cg = cooperative_groups;
     cg::cluster_group cluster = cg::this_cluster();
@@ -87,6 +89,7 @@ __global__ void __launch_bounds__(PC_THREADS, 1) k_power_cluster(PowerClusterPar
     const int a0 = (int)((int64_t)rank * m / CL), a1 = (int)((int64_t)(rank + 1) * m / CL);
     const int nrow = a1 - a0;
     // shared memory: v[ld] | y[2][ld] | part[2][CL][warps][4] float pairs | vprev[nrow] | r_own[nrow]
+    //                | (RES) rows[nrow][ld]
     auto a16 = [](size_t x) { return (x + 15) & ~size_t(15); };
     float* v = reinterpret_cast<float*>(dsm);
     float* ybuf = reinterpret_cast<float*>(dsm + a16((size_t)ld * 4));
@@ -98,13 +101,21 @@ __global__ void __launch_bounds__(PC_THREADS, 1) k_power_cluster(PowerClusterPar
     float* r_own = vprev + a16((size_t)nrow * 4) / 4;
     __shared__ double red[PC_THREADS / 32][4];
     __shared__ float sh_corr[2];
-    __shared__ double sh_inv;
+    __shared__ float sh_inv;
     __shared__ int sh_done;
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = PC_THREADS / 32;
     const double* rc = p.r + (size_t)c * m;
     const float* Sc = p.S + (size_t)c * m * ld;
     const double inv_m = 1.0 / (double)m, totc = p.tot[c];
+    const float finv_m = (float)inv_m, totf = (float)totc, tol2f = (float)p.tol2;
     for (int i = threadIdx.x; i < nrow; i += PC_THREADS) r_own[i] = (float)rc[a0 + i];
+    const int nv4 = ld / 4;
+    float4* srows = reinterpret_cast<float4*>(r_own + a16((size_t)nrow * 4) / 4);
+    if constexpr (RES) {
+        const float4* g = reinterpret_cast<const float4*>(Sc + (size_t)a0 * ld);
+        for (int e = threadIdx.x; e < nrow * nv4; e += PC_THREADS) srows[e] = __ldg(g + e);
+        // published by the barriers of the start-vector block below
+    }
 
     // v_0 = [1, .5, 1, .5, ...] / |.| (or the squaring's vector, normalised), with its
     // sum and r.v (identical in every CTA)
@@ -144,7 +155,7 @@ __global__ void __launch_bounds__(PC_THREADS, 1) k_power_cluster(PowerClusterPar
             const double inv = rsqrt_d(t2), sv = t1 * inv, rv = tr * inv;
             sh_corr[0] = (float)(-sv * inv_m);
             sh_corr[1] = (float)(-rv * inv_m + totc * sv * inv_m * inv_m);
-            sh_inv = inv;
+            sh_inv = (float)inv;
             sh_done = use;
         }
         __syncthreads();
@@ -165,7 +176,6 @@ __global__ void __launch_bounds__(PC_THREADS, 1) k_power_cluster(PowerClusterPar
     }
     cluster.sync();  // every CTA initialised before remote stores start
     int T = tmax;
-    const int nv4 = ld / 4;
     constexpr int U = BPL >= 8 ? 2 : PC_UNROLL;  // rows in flight per warp
     float fsc = 1.f;  // v_t = ybuf[(t-1)&1] * fsc for t >= 1 (the FP32 product the update stored before)
     for (int t = 0;; ++t) {
@@ -187,7 +197,8 @@ __global__ void __launch_bounds__(PC_THREADS, 1) k_power_cluster(PowerClusterPar
             for (int u = 0; u < U; ++u) {
                 s[u] = 0.f;
                 cp[u] = 0.f;
-                rowp[u] = reinterpret_cast<const float4*>(Sc + (size_t)(a0 + min(i0 + u, nrow - 1)) * ld);
+                rowp[u] = RES ? srows + (size_t)min(i0 + u, nrow - 1) * nv4
+                              : reinterpret_cast<const float4*>(Sc + (size_t)(a0 + min(i0 + u, nrow - 1)) * ld);
             }
             auto kahan4 = [&](int u, const float4& x, const float4& w) {
                 const float pr[4] = {x.x * w.x, x.y * w.y, x.z * w.z, x.w * w.w};
@@ -206,7 +217,7 @@ __global__ void __launch_bounds__(PC_THREADS, 1) k_power_cluster(PowerClusterPar
 #pragma unroll
                     for (int j = 0; j < BPL; ++j) {
                         const int b = lane + 32 * j;
-                        x[u][j] = b < nv4 ? __ldg(rowp[u] + b) : make_float4(0.f, 0.f, 0.f, 0.f);
+                        x[u][j] = b < nv4 ? (RES ? rowp[u][b] : __ldg(rowp[u] + b)) : make_float4(0.f, 0.f, 0.f, 0.f);
                     }
 #pragma unroll
                 for (int j = 0; j < BPL; ++j) {
@@ -230,7 +241,7 @@ __global__ void __launch_bounds__(PC_THREADS, 1) k_power_cluster(PowerClusterPar
                     w.w *= fsc;
                     float4 x[U];
 #pragma unroll
-                    for (int u = 0; u < U; ++u) x[u] = __ldg(rowp[u] + b);
+                    for (int u = 0; u < U; ++u) x[u] = RES ? rowp[u][b] : __ldg(rowp[u] + b);
 #pragma unroll
                     for (int u = 0; u < U; ++u) kahan4(u, x[u], w);
                 }
@@ -289,14 +300,15 @@ __global__ void __launch_bounds__(PC_THREADS, 1) k_power_cluster(PowerClusterPar
                     const float c2 = __shfl_xor_sync(0xffffffffu, tcm[q], o);
                     two_sum_acc(ts[q], tcm[q], s2, c2);
                 }
-            if (lane == 0) {
-                const double n2 = (double)ts[0] - (double)tcm[0], sy = (double)ts[1] - (double)tcm[1];
-                const double ry = (double)ts[2] - (double)tcm[2], dd = (double)ts[3] - (double)tcm[3];
-                const double inv = rsqrt_d(n2), sv = sy * inv, rv = ry * inv;
-                sh_corr[0] = (float)(-sv * inv_m);
-                sh_corr[1] = (float)(-rv * inv_m + totc * sv * inv_m * inv_m);
+            if (lane == 0) {  // FP32 (GB300's FP64 pipe is narrow and this is the step's critical path)
+                const float n2 = ts[0] - tcm[0], sy = ts[1] - tcm[1], ry = ts[2] - tcm[2], dd = ts[3] - tcm[3];
+                float inv = rsqrtf(n2);
+                inv = inv * fmaf(-0.5f * n2 * inv, inv, 1.5f);  // one Newton step: correctly rounded or 1 ulp
+                const float sv = sy * inv, rv = ry * inv;
+                sh_corr[0] = -sv * finv_m;
+                sh_corr[1] = fmaf(totf * finv_m * finv_m, sv, -rv * finv_m);
                 sh_inv = inv;
-                sh_done = t >= tmax || (t >= 1 && dd < p.tol2) || !(n2 > 0);
+                sh_done = t >= tmax || (t >= 1 && dd < tol2f) || !(n2 > 0.f);
             }
         }
         __syncthreads();
@@ -304,7 +316,7 @@ __global__ void __launch_bounds__(PC_THREADS, 1) k_power_cluster(PowerClusterPar
             T = t;
             break;
         }
-        fsc = (float)sh_inv;  // v_{t+1} = u_{t+1} * fsc, read from ybuf[par] in the next step
+        fsc = sh_inv;  // v_{t+1} = u_{t+1} * fsc, read from ybuf[par] in the next step
     }
     if (T >= 1) {  // materialise v_T = ybuf[(T-1)&1] * (its scale) for the final step
         const float* yv = ybuf + ((T - 1) & 1) * ld;
@@ -374,9 +386,9 @@ __global__ void __launch_bounds__(PC_THREADS, 1) k_power_cluster(PowerClusterPar
 }
 
 // ---------------------------------------------------------------- host
-template <int CL, int BPL>
+template <int CL, int BPL, bool RES>
 static void launch_cluster(const PowerClusterParams& pp, int k, size_t smem, cudaStream_t s) {
-    auto kern = k_power_cluster<CL, BPL>;
+    auto kern = k_power_cluster<CL, BPL, RES>;
     allow_max_dynamic_smem(kern);
     if (CL > 8) TC_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
     cudaLaunchConfig_t cfg = {};
@@ -396,12 +408,12 @@ static void launch_cluster(const PowerClusterParams& pp, int k, size_t smem, cud
 }
 
 template <int CL>
-static size_t cluster_smem(int m, int ld) {
+static size_t cluster_smem(int m, int ld, bool res) {
     auto a16 = [](size_t x) { return (x + 15) & ~size_t(15); };
     const int nrow = (m + CL - 1) / CL;
     constexpr int NWARP = PC_THREADS / 32;
     return a16((size_t)ld * 4) + a16((size_t)2 * ld * 4) + a16((size_t)2 * CL * NWARP * 4 * 8) + a16((size_t)nrow * 4) +
-           (size_t)nrow * 4;
+           a16((size_t)nrow * 4) + (res ? (size_t)nrow * ld * 4 : 0);
 }
 
 void power_eigvecs(tc_ctx* ctx, const float* S, int ld, const double* r, const double* tot, const int32_t* counts,
@@ -412,16 +424,25 @@ void power_eigvecs(tc_ctx* ctx, const float* S, int ld, const double* r, const d
                           tol * tol, steps, vinit, vok, tmax_sq};
     // long series stream tens of MB per step from HBM: spread each over 16 SMs
     if (m > 1024) {
-        const size_t smem = cluster_smem<16>(m, ld);
+        const size_t smem = cluster_smem<16>(m, ld, false);
         TC_REQUIRE(smem + 4096 <= ctx->smem_optin, TC_ERR_UNSUPPORTED, "power iteration: series too long");
-        launch_cluster<16, 0>(pp, k, smem, s);
+        launch_cluster<16, 0, false>(pp, k, smem, s);
     } else {
         const int nv4 = ld / 4;
-        const size_t smem = cluster_smem<8>(m, ld);
-        if (nv4 <= 32) launch_cluster<8, 1>(pp, k, smem, s);
-        else if (nv4 <= 64) launch_cluster<8, 2>(pp, k, smem, s);
-        else if (nv4 <= 128) launch_cluster<8, 4>(pp, k, smem, s);
-        else launch_cluster<8, 8>(pp, k, smem, s);
+        // rows resident in shared memory when they fit (4 KB left for the static arrays)
+        const bool res = cluster_smem<8>(m, ld, true) + 4096 <= ctx->smem_optin && !std::getenv("TIMESC_POWER_L2");
+        const size_t smem = cluster_smem<8>(m, ld, res);
+        if (res) {
+            if (nv4 <= 32) launch_cluster<8, 1, true>(pp, k, smem, s);
+            else if (nv4 <= 64) launch_cluster<8, 2, true>(pp, k, smem, s);
+            else if (nv4 <= 128) launch_cluster<8, 4, true>(pp, k, smem, s);
+            else launch_cluster<8, 8, true>(pp, k, smem, s);
+        } else {
+            if (nv4 <= 32) launch_cluster<8, 1, false>(pp, k, smem, s);
+            else if (nv4 <= 64) launch_cluster<8, 2, false>(pp, k, smem, s);
+            else if (nv4 <= 128) launch_cluster<8, 4, false>(pp, k, smem, s);
+            else launch_cluster<8, 8, false>(pp, k, smem, s);
+        }
     }
     cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
     TC_CUDA(cudaStreamIsCapturing(s, &cap));
