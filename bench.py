@@ -106,21 +106,33 @@ def profiled_traffic(workload, mode, prec):
 
 
 class Clocks:
-    """nvidia-smi sampling during the timed region."""
-    Q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+    """nvidia-smi sampling (every 20 ms, timestamped).  Start it before the warm-up
+    and bracket the timed region with begin()/end(): only samples inside that window
+    count (all samples when begin() was not called)."""
+    Q = ("timestamp,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
          "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
          "clocks_event_reasons.sw_power_cap")
 
     def __init__(self, device):
         self.f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+        self.t0 = self.t1 = None
         try:
             self.p = subprocess.Popen(["nvidia-smi", "-i", str(device), "--query-gpu=" + self.Q,
-                                       "--format=csv,noheader,nounits", "-lms", "200"],
+                                       "--format=csv,noheader,nounits", "-lms", "20"],
                                       stdout=self.f, stderr=subprocess.DEVNULL)
         except OSError:
             self.p = None
 
+    def begin(self):
+        import datetime
+        self.t0 = datetime.datetime.now()
+
+    def end(self):
+        import datetime
+        self.t1 = datetime.datetime.now()
+
     def stop(self):
+        import datetime
         if self.p is None:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
         self.p.terminate()
@@ -129,9 +141,23 @@ class Clocks:
         rows = []
         for line in open(self.f.name):
             parts = [t.strip() for t in line.split(",")]
-            if len(parts) == 7:
-                rows.append(parts)
+            if len(parts) != 8:
+                continue
+            try:
+                ts = datetime.datetime.strptime(parts[0], "%Y/%m/%d %H:%M:%S.%f")
+            except ValueError:
+                continue
+            rows.append((ts, parts[1:]))
         os.unlink(self.f.name)
+        window = "all samples"
+        if self.t0 is not None and self.t1 is not None:
+            lo, hi = self.t0 - datetime.timedelta(milliseconds=25), self.t1 + datetime.timedelta(milliseconds=25)
+            inside = [r for r in rows if lo <= r[0] <= hi]
+            if inside:
+                rows, window = inside, "timed region (%.0f ms)" % ((self.t1 - self.t0).total_seconds() * 1e3)
+            else:
+                window = "no sample inside the timed region: all samples (warm-up included)"
+        rows = [r[1] for r in rows]
         if not rows:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
         sm = [float(r[0]) for r in rows if r[0].replace(".", "").isdigit()]
@@ -139,7 +165,7 @@ class Clocks:
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
         reasons = sorted({names[j] for r in rows for j in range(4) if r[3 + j].lower() == "active"})
         return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
-                "reasons": reasons, "samples": len(rows)}
+                "reasons": reasons, "samples": len(rows), "window": window}
 
 
 def cufft_assign_ms(x, C, F, chunk=32768, reps=3):
@@ -356,9 +382,10 @@ def run_batched(args):
     specs = make_specs(timesc, sizes, prec, args.max_iter)
     warm = make_specs(timesc, sorted(sizes)[: min(16, len(sizes))], prec, 2, seed0=10_000)
     pool = timesc.Pool(device=0, workers=args.workers)
+    clk = Clocks(0)
     for _ in range(args.warmup):
         pool.run_batch(warm)
-    clk = Clocks(0)
+    clk.begin()
     l0 = timesc.lib().tc_launch_count()
     walls = []
     bad = []
@@ -367,6 +394,7 @@ def run_batched(args):
         st = pool.run_batch(specs)
         walls.append(time.perf_counter() - t0)
         bad += [i for i, v in enumerate(st) if v != timesc.OK]
+    clk.end()
     launches = timesc.lib().tc_launch_count() - l0
     clocks = clk.stop()
     pool.close()  # every job has ended before any failure is reported
@@ -426,6 +454,8 @@ def run_serving(args):
     tickets = [None] * len(specs)
     held = []
     clk = Clocks(0)
+    time.sleep(0.3)  # nvidia-smi up before the first request
+    clk.begin()
     start = time.perf_counter()
 
     def producer():
@@ -443,6 +473,7 @@ def run_serving(args):
     th.join()
     res = [pool.wait(t) for t in tickets]
     end = time.perf_counter()
+    clk.end()
     clocks = clk.stop()
     pool.close()  # every job has ended before any failure is reported
     assert all(r[0] == timesc.OK for r in res), [r[0] for r in res]
@@ -541,13 +572,14 @@ def main():
             rec[1].record(stream)
         return changed.item(), dsum.item()  # the reference reads its convergence flag back every iteration
 
+    clk = Clocks(local)  # sampling from the warm-up on; the timed window is marked below
     for _ in range(args.warmup):
         iteration()
     torch.cuda.synchronize()
     if dist:
         dist.barrier()
-    clk = Clocks(local)
     torch.cuda.synchronize()
+    clk.begin()
     l0 = timesc.lib().tc_launch_count()
     t_start = torch.cuda.Event(enable_timing=True)
     t_end = torch.cuda.Event(enable_timing=True)
@@ -556,6 +588,7 @@ def main():
         iteration(ev[s])
     t_end.record(stream)
     torch.cuda.synchronize()
+    clk.end()
     launches = timesc.lib().tc_launch_count() - l0
     clocks = clk.stop()
     ms = t_start.elapsed_time(t_end)
