@@ -16,8 +16,8 @@
 // so all CTAs hold bit-identical norms and take the same stop decision; clusters
 // stop independently.  Rank 0 finishes: Rayleigh quotient, sign rule, store.
 //
-// Arithmetic: row dot products are compensated FP32 (Kahan per lane, TwoSum
-// across lanes); the norm, the sums and the step difference are accumulated as
+// Arithmetic: row dot products are compensated FP32 (per lane, each float4's FMA
+// chain Kahan-added; TwoSum across lanes); the norm, the sums and the step difference are accumulated as
 // FP32 pairs (TwoSum, products split exactly by FMA: about 44 bits), so rounding
 // noise in |v_t - v_{t-1}| stays well below the tolerance; FP64 only for the
 // final per-step norm and corrections (one thread).
@@ -200,14 +200,13 @@ __global__ void __launch_bounds__(PC_THREADS, 1) k_power_cluster(PowerClusterPar
                 rowp[u] = RES ? srows + (size_t)min(i0 + u, nrow - 1) * nv4
                               : reinterpret_cast<const float4*>(Sc + (size_t)(a0 + min(i0 + u, nrow - 1)) * ld);
             }
+            // a float4's four products as one FMA chain (a few ulp of a 4-term partial),
+            // Kahan-added to the lane's sum: 8 operations where four Kahan additions take 20
             auto kahan4 = [&](int u, const float4& x, const float4& w) {
-                const float pr[4] = {x.x * w.x, x.y * w.y, x.z * w.z, x.w * w.w};
-#pragma unroll
-                for (int e = 0; e < 4; ++e) {
-                    const float yk = pr[e] - cp[u], tt = s[u] + yk;
-                    cp[u] = (tt - s[u]) - yk;
-                    s[u] = tt;
-                }
+                const float pr = fmaf(x.w, w.w, fmaf(x.z, w.z, fmaf(x.y, w.y, x.x * w.x)));
+                const float yk = pr - cp[u], tt = s[u] + yk;
+                cp[u] = (tt - s[u]) - yk;
+                s[u] = tt;
             };
             if constexpr (BPL > 0) {
                 // every load of the U rows in flight at once: one L2 round trip per step
