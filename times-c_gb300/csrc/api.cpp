@@ -377,6 +377,11 @@ int tc_create(int device, tc_ctx** out) {
         delete c;
         return TC_ERR_CUDA;
     }
+    if (cudaStreamCreateWithFlags(&c->copy_stream, cudaStreamNonBlocking) != cudaSuccess) {
+        cudaStreamDestroy(c->own_stream);
+        delete c;
+        return TC_ERR_CUDA;
+    }
     *out = c;
     return TC_OK;
 }
@@ -392,6 +397,7 @@ int tc_destroy(tc_ctx* ctx) {
         delete t;
     }
     cudaStreamDestroy(ctx->own_stream);
+    cudaStreamDestroy(ctx->copy_stream);
     delete ctx;
     return TC_OK;
 }
@@ -505,14 +511,36 @@ int tc_kshape_run(tc_ctx* ctx, const tc_job* job, tc_result* res) {
     const int64_t n = job->n;
     const int m = job->m, k = job->k;
     float* x = ctx->ws.x.as<float>((size_t)n * m);
-    if (job->h_data)
-        TC_CUDA(cudaMemcpyAsync(x, job->h_data, sizeof(float) * n * m, cudaMemcpyHostToDevice, s));
-    else
-        TC_CUDA(cudaMemcpyAsync(x, job->d_data, sizeof(float) * n * m, cudaMemcpyDeviceToDevice, s));
-    launch_znorm(x, n, m, 1, ctx->sm_count, s);  // test_kshape.cu:37 / :99
     // the series stay fixed for the whole run: their BF16 copy is made once
-    if (job->precision != TC_PREC_FP32 && tc_assign_supported(m, fft_size(m, job->mode), k, job->precision))
-        prepare_series_bf16(ctx, x, n, m, s);
+    const bool bf16 =
+        job->precision != TC_PREC_FP32 && tc_assign_supported(m, fft_size(m, job->mode), k, job->precision);
+    if (bf16) prepare_series_bf16_reserve(ctx, n, m);
+    // upload, z-norm (test_kshape.cu:37 / :99) and BF16 copy in row chunks: the copy
+    // stream uploads chunk i+1 while this stream normalises chunk i (rows are independent)
+    const int64_t chunk = std::max<int64_t>((n + 7) / 8, std::max<int64_t>(1, (16 << 20) / (4 * (int64_t)m)));
+    struct Events {  // destroyed on every exit; each is released once its recorded work completes
+        std::vector<cudaEvent_t> v;
+        ~Events() {
+            for (cudaEvent_t e : v) cudaEventDestroy(e);
+        }
+    } ev;
+    for (int64_t r0 = 0; r0 < n; r0 += chunk) {
+        const int64_t rows = std::min(chunk, n - r0);
+        const size_t off = (size_t)r0 * m, bytes = sizeof(float) * (size_t)rows * m;
+        if (job->h_data) {
+            cudaEvent_t e;
+            TC_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+            ev.v.push_back(e);
+            TC_CUDA(cudaMemcpyAsync(x + off, job->h_data + off, bytes, cudaMemcpyHostToDevice, ctx->copy_stream));
+            TC_CUDA(cudaEventRecord(e, ctx->copy_stream));
+            TC_CUDA(cudaStreamWaitEvent(s, e, 0));
+        } else {
+            TC_CUDA(cudaMemcpyAsync(x + off, job->d_data + off, bytes, cudaMemcpyDeviceToDevice, s));
+        }
+        launch_znorm(x + off, rows, m, 1, ctx->sm_count, s);
+        if (bf16) prepare_series_bf16_rows(ctx, x, n, m, r0, rows, s);
+    }
+    if (bf16) prepare_series_bf16_done(ctx, x, n, m);
     const int cap = job->max_iter > 0 ? job->max_iter : 20;
     LoopState st = run_loop(ctx, job, x, k, job->init_chose == 1, 0, cap, s);
     res->restarted = 0;

@@ -359,22 +359,38 @@ __global__ void __launch_bounds__(AT_THREADS, 1) k_assign_tc(const __grid_consta
 }
 
 // ---------------------------------------------------------------- host
-void prepare_series_bf16(tc_ctx* ctx, const float* x, int64_t n, int m, cudaStream_t s) {
+void prepare_series_bf16_reserve(tc_ctx* ctx, int64_t n, int m) {
     const int mp = (m + 63) / 64 * 64;
-    __nv_bfloat16* xb = ctx->ws.xbf.as<__nv_bfloat16>((size_t)n * mp);
-    float* xnorm = ctx->ws.xbf_norm.as<float>((size_t)n);
+    ctx->ws.xbf.as<__nv_bfloat16>((size_t)n * mp);
+    ctx->ws.xbf_norm.as<float>((size_t)n);
     ctx->prep_x = nullptr;
-    if (n > 0) {
-        const int wgrid = (int)std::min<int64_t>(ceil_div(n, 8), (int64_t)ctx->sm_count * 16);
-        if (m % 4 == 0 && reinterpret_cast<uintptr_t>(x) % 16 == 0)
-            k_series_bf16<true><<<wgrid, 256, 0, s>>>(x, n, m, mp, xb, xnorm);
-        else
-            k_series_bf16<false><<<wgrid, 256, 0, s>>>(x, n, m, mp, xb, xnorm);
-        TC_CHECK_LAUNCH();
-    }
+}
+
+void prepare_series_bf16_rows(tc_ctx* ctx, const float* x, int64_t n, int m, int64_t r0, int64_t rows,
+                              cudaStream_t s) {
+    const int mp = (m + 63) / 64 * 64;
+    __nv_bfloat16* xb = ctx->ws.xbf.as<__nv_bfloat16>((size_t)n * mp) + (size_t)r0 * mp;
+    float* xnorm = ctx->ws.xbf_norm.as<float>((size_t)n) + r0;
+    const float* xr = x + (size_t)r0 * m;
+    if (rows <= 0) return;
+    const int wgrid = (int)std::min<int64_t>(ceil_div(rows, 8), (int64_t)ctx->sm_count * 16);
+    if (m % 4 == 0 && reinterpret_cast<uintptr_t>(xr) % 16 == 0)
+        k_series_bf16<true><<<wgrid, 256, 0, s>>>(xr, rows, m, mp, xb, xnorm);
+    else
+        k_series_bf16<false><<<wgrid, 256, 0, s>>>(xr, rows, m, mp, xb, xnorm);
+    TC_CHECK_LAUNCH();
+}
+
+void prepare_series_bf16_done(tc_ctx* ctx, const float* x, int64_t n, int m) {
     ctx->prep_x = x;
     ctx->prep_n = n;
     ctx->prep_m = m;
+}
+
+void prepare_series_bf16(tc_ctx* ctx, const float* x, int64_t n, int m, cudaStream_t s) {
+    prepare_series_bf16_reserve(ctx, n, m);
+    prepare_series_bf16_rows(ctx, x, n, m, 0, n, s);
+    prepare_series_bf16_done(ctx, x, n, m);
 }
 
 bool tc_assign_supported(int m, int F, int k, int precision) {

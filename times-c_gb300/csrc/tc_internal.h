@@ -147,6 +147,7 @@ struct tc_ctx {
     std::vector<FftTables*> fft;  // cached per F
     Workspace ws;
     cudaStream_t own_stream = nullptr;
+    cudaStream_t copy_stream = nullptr;  // host uploads overlapped with own_stream's work
     // iteration stages replayed from CUDA graphs
     bool graphs = true;
     // launch plans picked by the autotuner, per kernel shape (see assign_fft.cu)
@@ -191,6 +192,11 @@ bool tc_assign_supported(int m, int F, int k, int precision);
 void launch_assign_tc(tc_ctx* ctx, const AssignArgs& a, int precision, cudaStream_t s);
 // BF16 copy and norms of the series into the context's workspace, marked as prepared for x
 void prepare_series_bf16(tc_ctx* ctx, const float* x, int64_t n, int m, cudaStream_t s);
+// the same in row ranges: reserve for n rows, convert [r0, r0 + rows), then mark x prepared
+void prepare_series_bf16_reserve(tc_ctx* ctx, int64_t n, int m);
+void prepare_series_bf16_rows(tc_ctx* ctx, const float* x, int64_t n, int m, int64_t r0, int64_t rows,
+                              cudaStream_t s);
+void prepare_series_bf16_done(tc_ctx* ctx, const float* x, int64_t n, int m);
 
 // extraction
 struct ExtractArgs {
