@@ -53,7 +53,12 @@ typedef enum {
 } tc_mode;
 
 typedef enum {
-    TC_PREC_FP32 = 0,      /* FP32 FFT correlation; Gram matrices in 3xTF32 on the tensor cores */
+    TC_PREC_FP32 = 0,      /* FP32 FFT correlation; Gram matrices in 3xTF32 on the tensor cores.  Where
+                              the BF16 correlation applies (FFT length 128..1024, k >= 2, no shift
+                              requested) a BF16 tensor-core pass first keeps, per series, only the
+                              centroids whose FP32 distance can be the minimum (a rigorous bound on
+                              the BF16 error); the FP32 pass evaluates those: same labels and
+                              distances as evaluating all (TIMESC_NO_SCREEN=1 turns it off) */
     TC_PREC_BF16 = 1,      /* BF16 operands, FP32 accumulation, on the tensor cores (tcgen05): the
                               correlation when FFT length is 128..1024 (m <= 512) and no shift is
                               requested (the FP32 FFT correlation otherwise), and the Gram matrices */
@@ -97,8 +102,8 @@ int tc_sbd_assign(tc_ctx* ctx, const float* d_x, const float* d_centroids, int64
 
 /* Keeps a BF16 copy of the series d_x (n rows of length m <= 512) and their FP32
  * norms in the context for the tensor-core correlation: later tc_sbd_assign calls
- * with TC_PREC_BF16 and the same d_x, n and m use it instead of converting the
- * series again.  The copy is taken now: call again after changing d_x.  Any
+ * with TC_PREC_BF16 (or TC_PREC_FP32, whose screening pass uses it) and the same
+ * d_x, n and m use it instead of converting the series again.  The copy is taken now: call again after changing d_x.  Any
  * tc_sbd_assign on other series, and tc_kshape_run, drop it.  No counterpart in
  * the reference (NCC_3D transforms the series on every iteration). */
 int tc_prepare_series(tc_ctx* ctx, const float* d_x, int64_t n, int m, tc_stream stream);

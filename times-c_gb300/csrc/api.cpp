@@ -69,7 +69,19 @@ static void assign(tc_ctx* ctx, const float* x, const float* C, int64_t n, int m
     a.old_labels = old;
     a.changed = changed;
     a.dist_sum = dsum;
-    if (precision == TC_PREC_FP32 || shift || !tc_assign_supported(m, F, k, precision)) {
+    if (precision == TC_PREC_FP32 && !shift && screen_supported(m, F, k)) {
+        // exact screening: the BF16 pass keeps every centroid whose FP32 distance can be
+        // the minimum, the FP32 pass evaluates those (same labels and distances as the
+        // unscreened FP32 kernel)
+        a.centroids = C;
+        a.cand = ctx->ws.screen.as<int32_t>((size_t)n * (SCREEN_CAP + 1));
+        a.ncand = a.cand + (size_t)n * SCREEN_CAP;
+        launch_assign_tc(ctx, a, TC_PREC_BF16, s);
+        float2* spec = ctx->ws.spectra.as<float2>((size_t)k * (F / 2 + 1));
+        launch_centroid_spectra(ctx, C, k, m, F, spec, s);
+        a.spec = spec;
+        launch_assign_fft(ctx, a, s);
+    } else if (precision == TC_PREC_FP32 || shift || !tc_assign_supported(m, F, k, precision)) {
         float2* spec = ctx->ws.spectra.as<float2>((size_t)k * (F / 2 + 1));
         launch_centroid_spectra(ctx, C, k, m, F, spec, s);
         a.spec = spec;
@@ -282,7 +294,7 @@ static LoopState run_loop(tc_ctx* ctx, const tc_job* job, const float* x, int k,
 static const char* const WS_NAMES[] = {"x", "labels", "old_labels", "shift", "dist", "centroids", "spectra",
                                        "seg", "perm", "chunk_counts", "counts", "offsets", "gate", "scal",
                                        "gram", "rowsum", "gram_yt", "gram_poff", "piter", "pstats", "aux",
-                                       "toeplitz", "toeplitz_norm", "xbf", "xbf_norm", "first", "gram_sq", "sq_meta"};
+                                       "toeplitz", "toeplitz_norm", "xbf", "xbf_norm", "first", "gram_sq", "sq_meta", "screen"};
 
 static std::vector<DevBuf*> workspace_buffers(tc_ctx* ctx);
 
@@ -318,7 +330,7 @@ static std::vector<DevBuf*> workspace_buffers(tc_ctx* ctx) {
     return {&w.x,    &w.labels,  &w.old_labels, &w.shift,   &w.dist,      &w.centroids, &w.spectra,
             &w.seg,  &w.perm,    &w.chunk_counts, &w.counts, &w.offsets,  &w.gate,      &w.scal,
             &w.gram, &w.rowsum,  &w.gram_yt,    &w.gram_poff, &w.piter,   &w.pstats,    &w.aux,
-            &w.toeplitz, &w.toeplitz_norm, &w.xbf, &w.xbf_norm, &w.first, &w.gram_sq, &w.sq_meta};
+            &w.toeplitz, &w.toeplitz_norm, &w.xbf, &w.xbf_norm, &w.first, &w.gram_sq, &w.sq_meta, &w.screen};
 }
 
 void release_workspace(tc_ctx* ctx) {
@@ -445,7 +457,8 @@ int tc_sbd_assign(tc_ctx* ctx, const float* d_x, const float* d_centroids, int64
     TC_CUDA(cudaMemsetAsync(words, 0, 2 * sizeof(int), s));
     assign(ctx, d_x, d_centroids, n, m, k, mode, precision, d_labels, d_dist, d_shift, d_old_labels, d_changed,
            d_dist_sum, s);
-    if (precision != TC_PREC_FP32) {  // the tensor-core path reports through an error word
+    const bool tc_used = precision != TC_PREC_FP32 || (!d_shift && screen_supported(m, fft_size(m, mode), k));
+    if (tc_used) {  // the tensor-core pass reports through an error word
         int h[2] = {0, 0};
         TC_CUDA(cudaMemcpyAsync(h, words, sizeof(h), cudaMemcpyDeviceToHost, s));
         TC_CUDA(cudaStreamSynchronize(s));
@@ -512,8 +525,9 @@ int tc_kshape_run(tc_ctx* ctx, const tc_job* job, tc_result* res) {
     const int m = job->m, k = job->k;
     float* x = ctx->ws.x.as<float>((size_t)n * m);
     // the series stay fixed for the whole run: their BF16 copy is made once
-    const bool bf16 =
-        job->precision != TC_PREC_FP32 && tc_assign_supported(m, fft_size(m, job->mode), k, job->precision);
+    const int F = fft_size(m, job->mode);
+    const bool bf16 = (job->precision != TC_PREC_FP32 && tc_assign_supported(m, F, k, job->precision)) ||
+                      (job->precision == TC_PREC_FP32 && screen_supported(m, F, k));
     if (bf16) prepare_series_bf16_reserve(ctx, n, m);
     // upload, z-norm (test_kshape.cu:37 / :99) and BF16 copy in row chunks: the copy
     // stream uploads chunk i+1 while this stream normalises chunk i (rows are independent)

@@ -211,6 +211,9 @@ struct AssignParams {
     const int32_t* old_labels;
     int32_t* changed;
     double* dist_sum;
+    // screened assignment: only centroids cand[i][0 .. ncand[i]) (ascending; -1: all)
+    const int32_t* cand;
+    const int32_t* ncand;
 };
 
 // Max NCC over the valid lags with the lag of the first maximum in sbd3D's order
@@ -276,9 +279,19 @@ __global__ void __launch_bounds__(Cfg<N>::BLOCK, 1) k_assign_fft(AssignParams p)
             c0 = p.fixed[i];
             c1 = c0 + 1;
         }
+        // screened: the candidates in ascending order (every centroid that can be the
+        // first minimum), so the first strict minimum below is the unscreened one
+        const int32_t* cl = nullptr;
+        int ncl = -1;
+        if (p.cand) {
+            ncl = p.ncand[i];
+            cl = p.cand + (size_t)i * SCREEN_CAP;
+        }
+        const int iters = ncl >= 0 ? ncl : c1 - c0;
         float bestd = 1e10f;  // get_pos_idx: min_val = 1e10, pos = 0
         int bestj = 0, bests = 0;
-        for (int c = c0; c < c1; ++c) {
+        for (int it = 0; it < iters; ++it) {
+            const int c = ncl >= 0 ? cl[it] : c0 + it;
             float2 v[2][Co::R0];
             if (CSMEM) {
                 const float2* S = cspec + (size_t)c * (N + 1);
@@ -380,7 +393,7 @@ template <int N, bool SHIFT>
 static AssignPlan tuned_plan(tc_ctx* ctx, const AssignParams& p, cudaStream_t s) {
     const bool fits = Cfg<N>::smem(p.k, true) <= ctx->smem_optin;
     const AssignPlan dflt{fits, 0};
-    const uint64_t key = ((uint64_t)N << 40) | ((uint64_t)p.k << 8) | (SHIFT ? 1u : 0u);
+    const uint64_t key = ((uint64_t)N << 40) | ((uint64_t)p.k << 8) | (SHIFT ? 1u : 0u) | (p.cand ? 2u : 0u);
     for (const auto& t : ctx->tuned)
         if (t.first == key) return AssignPlan{(t.second & 1u) != 0, (int)(t.second >> 1)};
     const char* env = std::getenv("TIMESC_AUTOTUNE");
@@ -456,6 +469,8 @@ static void assign_n(tc_ctx* ctx, const AssignArgs& a, cudaStream_t s) {
     p.old_labels = a.old_labels;
     p.changed = a.changed;
     p.dist_sum = a.dist_sum;
+    p.cand = a.cand;
+    p.ncand = a.ncand;
     const bool want_shift = a.shift != nullptr || a.fixed != nullptr;
     if (want_shift) launch_plan<N, true>(ctx, p, tuned_plan<N, true>(ctx, p, s), s);
     else launch_plan<N, false>(ctx, p, tuned_plan<N, false>(ctx, p, s), s);

@@ -30,6 +30,8 @@
 #include <cuda_bf16.h>
 
 #include <algorithm>
+#include <cmath>
+#include <cstdlib>
 #include <vector>
 
 #include "sm100.cuh"
@@ -155,7 +157,30 @@ struct AtParams {
     int32_t* changed;
     double* dist_sum;
     int* err;
+    // screening (labels etc. unused): per series the centroids with d <= best + thr,
+    // ascending, at most SCREEN_CAP (count -1: more, evaluate all)
+    int32_t* cand;
+    int32_t* ncand;
+    float thr;
 };
+
+// Keep the list entries with distance <= lim (NaN kept), in order; returns the count.
+// Unrolled with constant indices so the lists stay in registers.
+__device__ __forceinline__ int screen_compact(int (&cj)[SCREEN_CAP], float (&cd)[SCREEN_CAP], int nc, float lim) {
+    int w = 0;
+#pragma unroll
+    for (int t = 0; t < SCREEN_CAP; ++t) {
+        const bool keep = t < nc && !(cd[t] > lim);
+#pragma unroll
+        for (int u = 0; u <= t; ++u)
+            if (keep && u == w) {
+                cj[u] = cj[t];
+                cd[u] = cd[t];
+            }
+        w += keep ? 1 : 0;
+    }
+    return w;
+}
 
 __global__ void __launch_bounds__(AT_THREADS, 1) k_assign_tc(const __grid_constant__ CUtensorMap tmapX, AtParams p) {
     extern __shared__ uint8_t smem_raw[];
@@ -296,6 +321,14 @@ __global__ void __launch_bounds__(AT_THREADS, 1) k_assign_tc(const __grid_consta
             const float xn = i < p.n ? p.xnorm[i] : 0.f;
             float bestd = 1e10f;  // get_pos_idx: min_val = 1e10, pos = 0
             int bestj = 0;
+            int cj[SCREEN_CAP];
+            float cd[SCREEN_CAP];
+#pragma unroll
+            for (int t = 0; t < SCREEN_CAP; ++t) {
+                cj[t] = 0;
+                cd[t] = 0.f;
+            }
+            int nc = 0;  // -1: the list overflowed
             for (int j = 0; j < p.k && ok; ++j) {
                 float mx = -3.0e38f;
                 for (int h = 0; h < g.H && ok; ++h, ++q) {
@@ -335,12 +368,34 @@ __global__ void __launch_bounds__(AT_THREADS, 1) k_assign_tc(const __grid_consta
                     bestd = d;
                     bestj = j;
                 }
+                if (p.cand && nc >= 0 && !(d > bestd + p.thr)) {
+                    if (nc == SCREEN_CAP) nc = screen_compact(cj, cd, nc, bestd + p.thr);
+                    if (nc == SCREEN_CAP) {
+                        nc = -1;
+                    } else {
+#pragma unroll
+                        for (int t = 0; t < SCREEN_CAP; ++t)
+                            if (t == nc) {
+                                cj[t] = j;
+                                cd[t] = d;
+                            }
+                        ++nc;
+                    }
+                }
             }
             if (ok && i < p.n) {
-                if (p.labels) p.labels[i] = bestj;
-                if (p.dist) p.dist[i] = bestd;
-                dsum += (double)bestd;
-                if (p.old_labels && p.old_labels[i] != bestj) ++nchg;
+                if (p.cand) {
+                    if (nc >= 0) nc = screen_compact(cj, cd, nc, bestd + p.thr);
+                    int4* o = reinterpret_cast<int4*>(p.cand + (size_t)i * SCREEN_CAP);
+                    o[0] = make_int4(cj[0], cj[1], cj[2], cj[3]);
+                    o[1] = make_int4(cj[4], cj[5], cj[6], cj[7]);
+                    p.ncand[i] = nc;
+                } else {
+                    if (p.labels) p.labels[i] = bestj;
+                    if (p.dist) p.dist[i] = bestd;
+                    dsum += (double)bestd;
+                    if (p.old_labels && p.old_labels[i] != bestj) ++nchg;
+                }
             }
         }
 #pragma unroll
@@ -397,6 +452,23 @@ bool tc_assign_supported(int m, int F, int k, int precision) {
     return precision == TC_PREC_BF16 && m >= 2 && m <= 512 && F >= 128 && F <= 1024 && k >= 1;
 }
 
+bool screen_supported(int m, int F, int k) {
+    return !std::getenv("TIMESC_NO_SCREEN") && k >= 2 && tc_assign_supported(m, F, k, TC_PREC_BF16);
+}
+
+// Bound on |d_BF16 - d_FP32| for one (series, centroid) pair.  With x~ = x(1+e1),
+// c~ = c(1+e2), |e| <= 2^-9 (BF16 rounding), every lag's |x~.c~ - x.c| <= (2^-8 + 2^-18)
+// sum |x_i c_j| <= (2^-8 + 2^-18) |x||c| (Cauchy-Schwarz); the norms are FP32 in both
+// kernels.  Allowances: tensor-core FP32 accumulation over mp terms (mp * 2^-21, with
+// room for truncating adders) and the FP32 FFT kernel's own error (1e-5).  A max over
+// lags and the clamp at 2 do not widen it.  If d32(j*) is the FP32 minimum and d16(jb)
+// the BF16 one, d16(j*) <= d32(j*) + D <= d32(jb) + D <= d16(jb) + 2D: every centroid
+// that can be the FP32 first minimum (ties included) has d16 <= min d16 + 2D.
+static float screen_threshold(int mp) {
+    const double D = std::ldexp(1.0, -8) + std::ldexp(1.0, -18) + mp * std::ldexp(1.0, -21) + 1e-5;
+    return (float)(2.0 * D * (1.0 + 1e-3));
+}
+
 void launch_assign_tc(tc_ctx* ctx, const AssignArgs& a, int precision, cudaStream_t s) {
     TC_REQUIRE(tc_assign_supported(a.m, a.F, a.k, precision), TC_ERR_UNSUPPORTED, "tensor-core correlation shape");
     if (a.n == 0) return;
@@ -431,6 +503,16 @@ void launch_assign_tc(tc_ctx* ctx, const AssignArgs& a, int precision, cudaStrea
     p.changed = a.changed;
     p.dist_sum = a.dist_sum;
     p.err = err;
+    if (a.cand) {
+        p.cand = a.cand;
+        p.ncand = a.ncand;
+        p.thr = screen_threshold(g.mp);
+        p.labels = nullptr;
+        p.dist = nullptr;
+        p.old_labels = nullptr;
+        p.changed = nullptr;
+        p.dist_sum = nullptr;
+    }
     const size_t smem = g.smem();
     allow_max_dynamic_smem(k_assign_tc);
     const int64_t ntiles = (a.n + AT_TILE - 1) / AT_TILE;

@@ -184,11 +184,13 @@ uint64_t tc_job_footprint(const tc_job* j) {
     const uint64_t mp64 = (m + 63) / 64 * 64;
     const uint64_t Psq = std::max<uint64_t>((k * mp64 + 63 * k + 63) / 64 * 64, 64);
     b += std::max(m * Pp * esize * planes, m * Psq * 8);  // Gram operand (members, or the squared matrices)
-    if (j->precision != TC_PREC_FP32 && tc::tc_assign_supported(j->m, (int)F, j->k, j->precision)) {
+    const bool screened = j->precision == TC_PREC_FP32 && tc::screen_supported(j->m, (int)F, j->k);
+    if ((j->precision != TC_PREC_FP32 && tc::tc_assign_supported(j->m, (int)F, j->k, j->precision)) || screened) {
         const uint64_t mp = (m + 63) / 64 * 64;
         b += n * mp * 2 + n * 4;           // BF16 series and norms
         b += k * (F / 8) * (mp + 56) * 2 + k * 4;  // shifted centroid buffers
     }
+    if (screened) b += n * (tc::SCREEN_CAP + 1) * 4;  // candidate lists
     b += ((n + 4095) / 4096) * k * 4;      // segment chunk counts
     return b + (1u << 20);
 }

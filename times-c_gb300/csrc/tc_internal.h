@@ -137,6 +137,7 @@ struct Workspace {
     DevBuf toeplitz_norm;  // k f32 centroid norms
     DevBuf xbf;          // bf16 copy of the series for the tensor-core correlation
     DevBuf xbf_norm;     // n f32 series norms
+    DevBuf screen;       // n x SCREEN_CAP candidate centroids + n counts (screened FP32 assignment)
 };
 
 struct tc_ctx {
@@ -184,11 +185,19 @@ struct AssignArgs {
     const int32_t* old_labels;
     int32_t* changed;
     double* dist_sum;
+    // exact screening of the FP32 assignment: the tensor-core pass writes, per series,
+    // up to SCREEN_CAP candidate centroids in ascending order (ncand -1: all), and the
+    // FFT pass evaluates only those
+    int32_t* cand;
+    int32_t* ncand;
 };
+constexpr int SCREEN_CAP = 8;
 void launch_assign_fft(tc_ctx* ctx, const AssignArgs& a, cudaStream_t s);
 
 // tensor-core correlation (tcgen05); returns false when the shape is not supported
 bool tc_assign_supported(int m, int F, int k, int precision);
+// the FP32 assignment screened by the BF16 tensor-core pass (TIMESC_NO_SCREEN turns it off)
+bool screen_supported(int m, int F, int k);
 void launch_assign_tc(tc_ctx* ctx, const AssignArgs& a, int precision, cudaStream_t s);
 // BF16 copy and norms of the series into the context's workspace, marked as prepared for x
 void prepare_series_bf16(tc_ctx* ctx, const float* x, int64_t n, int m, cudaStream_t s);
