@@ -172,12 +172,14 @@ __global__ void __launch_bounds__(128, 1) k_gram_tc(const __grid_constant__ CUte
             if (u > 0) ok = sm100::mbar_wait(&empty[s], (u - 1) & 1, err);
             if (!ok) break;
             uint8_t* A = base + (size_t)s * G::TILES * GT_TILE_BYTES;  // [A | B | A_lo | B_lo]
-            sm100::mbar_expect_tx(&full[s], G::TILES * GT_TILE_BYTES);
+            // a diagonal tile's B is its A: loaded once
+            sm100::mbar_expect_tx(&full[s], (ta == tb ? G::TILES / 2 : G::TILES) * GT_TILE_BYTES);
             sm100::tma_load_2d(A, &tmap, x0 + kb * KE, ta * GT_TILE, &full[s]);
-            sm100::tma_load_2d(A + GT_TILE_BYTES, &tmap, x0 + kb * KE, tb * GT_TILE, &full[s]);
+            if (ta != tb) sm100::tma_load_2d(A + GT_TILE_BYTES, &tmap, x0 + kb * KE, tb * GT_TILE, &full[s]);
             if (FMT == 3) {
                 sm100::tma_load_2d(A + 2 * GT_TILE_BYTES, &tmap_lo, x0 + kb * KE, ta * GT_TILE, &full[s]);
-                sm100::tma_load_2d(A + 3 * GT_TILE_BYTES, &tmap_lo, x0 + kb * KE, tb * GT_TILE, &full[s]);
+                if (ta != tb)
+                    sm100::tma_load_2d(A + 3 * GT_TILE_BYTES, &tmap_lo, x0 + kb * KE, tb * GT_TILE, &full[s]);
             }
         }
         // the MMA thread's last commits to empty[] arrive when their MMAs end: wait for
@@ -195,7 +197,8 @@ __global__ void __launch_bounds__(128, 1) k_gram_tc(const __grid_constant__ CUte
             if (!ok) break;
             sm100::tc_fence_after();
             uint8_t* A = base + (size_t)s * G::TILES * GT_TILE_BYTES;
-            const uint64_t da = sm100::desc_k_sw128(A), db = sm100::desc_k_sw128(A + GT_TILE_BYTES);
+            const int bo = ta == tb ? 0 : GT_TILE_BYTES;  // a diagonal tile's B is its A
+            const uint64_t da = sm100::desc_k_sw128(A), db = sm100::desc_k_sw128(A + bo);
 #pragma unroll
             for (int kk = 0; kk < 4; ++kk) {  // 4 x 32 bytes of K per slab
                 if (FMT == 1) {
@@ -204,7 +207,7 @@ __global__ void __launch_bounds__(128, 1) k_gram_tc(const __grid_constant__ CUte
                     sm100::mma_tf32(tmem, da + 2 * kk, db + 2 * kk, ID, (kb | kk) != 0);
                     if (FMT == 3) {
                         const uint64_t dal = sm100::desc_k_sw128(A + 2 * GT_TILE_BYTES);
-                        const uint64_t dbl = sm100::desc_k_sw128(A + 3 * GT_TILE_BYTES);
+                        const uint64_t dbl = sm100::desc_k_sw128(A + 2 * GT_TILE_BYTES + bo);
                         sm100::mma_tf32(tmem, da + 2 * kk, dbl + 2 * kk, ID, 1);
                         sm100::mma_tf32(tmem, dal + 2 * kk, db + 2 * kk, ID, 1);
                     }
@@ -226,10 +229,11 @@ __global__ void __launch_bounds__(128, 1) k_gram_tc(const __grid_constant__ CUte
             sm100::tmem_ld32(tmem + ((uint32_t)(warp * 32) << 16) + cb * 32, r);
             sm100::tmem_ld_wait();
             const int b0 = tb * GT_TILE + cb * 32;
-            if (a < m) {
+            if (a < m) {  // the row's 32 values as float4 (columns m..ld-1 are products with zero rows: 0)
+                float4* row4 = reinterpret_cast<float4*>(Sc + (size_t)a * ld + b0);
 #pragma unroll
-                for (int j = 0; j < 32; ++j)
-                    if (b0 + j < m) Sc[(size_t)a * ld + b0 + j] = r[j];
+                for (int q = 0; q < 8; ++q)
+                    if (b0 + 4 * q < ld) row4[q] = make_float4(r[4 * q], r[4 * q + 1], r[4 * q + 2], r[4 * q + 3]);
             }
             if (ta != tb) {
 #pragma unroll
