@@ -294,7 +294,7 @@ static LoopState run_loop(tc_ctx* ctx, const tc_job* job, const float* x, int k,
 static const char* const WS_NAMES[] = {"x", "labels", "old_labels", "shift", "dist", "centroids", "spectra",
                                        "seg", "perm", "chunk_counts", "counts", "offsets", "gate", "scal",
                                        "gram", "rowsum", "gram_yt", "gram_poff", "piter", "pstats", "aux",
-                                       "toeplitz", "toeplitz_norm", "xbf", "xbf_norm", "first", "gram_sq", "sq_meta", "screen"};
+                                       "toeplitz", "toeplitz_norm", "xbf", "xbf_norm", "first", "gram_sq", "sq_meta", "screen", "gram_part"};
 
 static std::vector<DevBuf*> workspace_buffers(tc_ctx* ctx);
 
@@ -330,7 +330,7 @@ static std::vector<DevBuf*> workspace_buffers(tc_ctx* ctx) {
     return {&w.x,    &w.labels,  &w.old_labels, &w.shift,   &w.dist,      &w.centroids, &w.spectra,
             &w.seg,  &w.perm,    &w.chunk_counts, &w.counts, &w.offsets,  &w.gate,      &w.scal,
             &w.gram, &w.rowsum,  &w.gram_yt,    &w.gram_poff, &w.piter,   &w.pstats,    &w.aux,
-            &w.toeplitz, &w.toeplitz_norm, &w.xbf, &w.xbf_norm, &w.first, &w.gram_sq, &w.sq_meta, &w.screen};
+            &w.toeplitz, &w.toeplitz_norm, &w.xbf, &w.xbf_norm, &w.first, &w.gram_sq, &w.sq_meta, &w.screen, &w.gram_part};
 }
 
 void release_workspace(tc_ctx* ctx) {

@@ -176,7 +176,7 @@ uint64_t tc_job_footprint(const tc_job* j) {
     b += n * m * 4;                        // members in cluster order
     b += n * 4 * 5;                        // labels, old labels, shifts, distances, permutation
     b += k * m * 4 + k * (F / 2 + 1) * 8;  // centroids, spectra
-    b += 2 * k * m * ld * 4;               // Gram matrices and their squares (power by squaring)
+    b += 6 * k * m * ld * 4;               // Gram matrices, their K-share partials (<= 4), squares
     b += (k * m + k) * 8 + 3 * k * m * 4;  // row sums, power-iteration vectors
     b += k * 8 * 4;                        // counts, offsets, padded offsets, gates
     const uint64_t esize = j->precision == TC_PREC_BF16 ? 2 : 4;

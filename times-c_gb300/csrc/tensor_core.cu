@@ -17,6 +17,7 @@
 #include <cuda_bf16.h>
 
 #include <algorithm>
+#include <cmath>
 #include <cstdlib>
 #include <vector>
 
@@ -130,7 +131,8 @@ __global__ void __launch_bounds__(128, 1) k_gram_tc(const __grid_constant__ CUte
                                                     const __grid_constant__ CUtensorMap tmap_lo,
                                                     const int32_t* __restrict__ counts,
                                                     const int64_t* __restrict__ poff, int m, int ld, int nt,
-                                                    float* __restrict__ S, int* __restrict__ err) {
+                                                    int nsplit, size_t part_stride, float* __restrict__ S,
+                                                    int* __restrict__ err) {
     extern __shared__ uint8_t smem_raw[];
     typedef GtCfg<FMT> G;
     __shared__ __align__(8) uint64_t full[G::STAGES], empty[G::STAGES], done;
@@ -143,7 +145,10 @@ __global__ void __launch_bounds__(128, 1) k_gram_tc(const __grid_constant__ CUte
     while (t >= nt - ta) { t -= nt - ta; ++ta; }
     const int tb = ta + t;
     constexpr int KE = G::KE;
-    const int nk = (cnt + KE - 1) / KE;
+    // split K: this CTA's share of the cluster's K blocks, into partial buffer z
+    const int nk_all = (cnt + KE - 1) / KE, z = blockIdx.z;
+    const int kb0 = (int)((int64_t)z * nk_all / nsplit), nk = (int)((int64_t)(z + 1) * nk_all / nsplit) - kb0;
+    if (nk == 0) return;  // the sum kernel skips empty shares
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     if (threadIdx.x == 0) {
         for (int s = 0; s < G::STAGES; ++s) {
@@ -174,12 +179,12 @@ __global__ void __launch_bounds__(128, 1) k_gram_tc(const __grid_constant__ CUte
             uint8_t* A = base + (size_t)s * G::TILES * GT_TILE_BYTES;  // [A | B | A_lo | B_lo]
             // a diagonal tile's B is its A: loaded once
             sm100::mbar_expect_tx(&full[s], (ta == tb ? G::TILES / 2 : G::TILES) * GT_TILE_BYTES);
-            sm100::tma_load_2d(A, &tmap, x0 + kb * KE, ta * GT_TILE, &full[s]);
-            if (ta != tb) sm100::tma_load_2d(A + GT_TILE_BYTES, &tmap, x0 + kb * KE, tb * GT_TILE, &full[s]);
+            const int xk = x0 + (kb0 + kb) * KE;
+            sm100::tma_load_2d(A, &tmap, xk, ta * GT_TILE, &full[s]);
+            if (ta != tb) sm100::tma_load_2d(A + GT_TILE_BYTES, &tmap, xk, tb * GT_TILE, &full[s]);
             if (FMT == 3) {
-                sm100::tma_load_2d(A + 2 * GT_TILE_BYTES, &tmap_lo, x0 + kb * KE, ta * GT_TILE, &full[s]);
-                if (ta != tb)
-                    sm100::tma_load_2d(A + 3 * GT_TILE_BYTES, &tmap_lo, x0 + kb * KE, tb * GT_TILE, &full[s]);
+                sm100::tma_load_2d(A + 2 * GT_TILE_BYTES, &tmap_lo, xk, ta * GT_TILE, &full[s]);
+                if (ta != tb) sm100::tma_load_2d(A + 3 * GT_TILE_BYTES, &tmap_lo, xk, tb * GT_TILE, &full[s]);
             }
         }
         // the MMA thread's last commits to empty[] arrive when their MMAs end: wait for
@@ -223,7 +228,7 @@ __global__ void __launch_bounds__(128, 1) k_gram_tc(const __grid_constant__ CUte
     sm100::tc_fence_after();
     if (fin) {
         const int a = ta * GT_TILE + warp * 32 + lane;
-        float* Sc = S + (size_t)c * m * ld;
+        float* Sc = S + (size_t)z * part_stride + (size_t)c * m * ld;
         for (int cb = 0; cb < 4; ++cb) {
             float r[32];
             sm100::tmem_ld32(tmem + ((uint32_t)(warp * 32) << 16) + cb * 32, r);
@@ -248,6 +253,32 @@ __global__ void __launch_bounds__(128, 1) k_gram_tc(const __grid_constant__ CUte
     sm100::tc_fence_before();
     __syncthreads();
     if (warp == 0) sm100::tmem_dealloc(tmem, 128);
+}
+
+// S_c = sum of the K shares' partial Grams, in share order (deterministic); shares
+// with no K blocks wrote nothing and are skipped.  Rows a < m, columns < ld (the
+// padding columns are zeros in every partial).
+__global__ void k_gram_sum(const float* __restrict__ P, int nsplit, size_t part_stride,
+                           const int32_t* __restrict__ counts, int KE, int m, int ld, float* __restrict__ S) {
+    const int c = blockIdx.y;
+    const int cnt = counts[c];
+    if (cnt == 0) return;
+    const int nk = (cnt + KE - 1) / KE;
+    const size_t n4 = (size_t)m * ld / 4, off = (size_t)c * m * ld / 4;
+    const float4* P4 = reinterpret_cast<const float4*>(P);
+    float4* S4 = reinterpret_cast<float4*>(S);
+    for (size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x; e < n4; e += (size_t)gridDim.x * blockDim.x) {
+        float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
+        for (int z = 0; z < nsplit; ++z) {
+            if ((int64_t)(z + 1) * nk / nsplit == (int64_t)z * nk / nsplit) continue;
+            const float4 q = P4[z * (part_stride / 4) + off + e];
+            v.x += q.x;
+            v.y += q.y;
+            v.z += q.z;
+            v.w += q.w;
+        }
+        S4[off + e] = v;
+    }
 }
 
 // ---------------------------------------------------------------- host
@@ -328,18 +359,42 @@ void launch_gram_tc(tc_ctx* ctx, const float* seg, const int32_t* counts, const 
     CUtensorMap map = make_tmap_2d(YT, dt, esize, (uint64_t)m, (uint64_t)Pp, GT_TILE);
     CUtensorMap map_lo = fmt == 3 ? make_tmap_2d(YTlo, dt, esize, (uint64_t)m, (uint64_t)Pp, GT_TILE) : map;
     const int nt = ceil_div(m, GT_TILE);
-    dim3 grid(nt * (nt + 1) / 2, k);
+    // K split across CTAs so the launch fills its last wave (one CTA per SM: the
+    // operand ring takes most of the shared memory): the share count with the best
+    // wave occupancy, each share keeping at least 32 K blocks on average
+    const int KE = fmt == 1 ? GtCfg<1>::KE : GtCfg<3>::KE;
+    const int units = nt * (nt + 1) / 2 * k;
+    const int64_t avg_kb = std::max<int64_t>(1, n / std::max(k, 1) / KE);
+    auto occupancy = [&](int sp) {
+        const double x = (double)units * sp / ctx->sm_count;
+        return x / std::ceil(x);
+    };
+    int nsplit = 1;
+    for (int sp = 2; sp <= 4 && avg_kb / sp >= 32; ++sp)
+        if (occupancy(sp) > occupancy(nsplit) + 0.02) nsplit = sp;
+    if (std::getenv("TIMESC_GRAM_NOSPLIT")) nsplit = 1;
+    const size_t part_stride = (size_t)k * m * ld;
+    float* out = nsplit > 1 ? ctx->ws.gram_part.as<float>((size_t)nsplit * part_stride) : S;
+    dim3 grid(nt * (nt + 1) / 2, k, nsplit);
     if (fmt == 1) {
         allow_max_dynamic_smem(k_gram_tc<1>);
-        k_gram_tc<1><<<grid, 128, GtCfg<1>::SMEM, s>>>(map, map_lo, counts, poff, m, ld, nt, S, err);
+        k_gram_tc<1><<<grid, 128, GtCfg<1>::SMEM, s>>>(map, map_lo, counts, poff, m, ld, nt, nsplit, part_stride,
+                                                        out, err);
     } else if (fmt == 2) {
         allow_max_dynamic_smem(k_gram_tc<2>);
-        k_gram_tc<2><<<grid, 128, GtCfg<2>::SMEM, s>>>(map, map_lo, counts, poff, m, ld, nt, S, err);
+        k_gram_tc<2><<<grid, 128, GtCfg<2>::SMEM, s>>>(map, map_lo, counts, poff, m, ld, nt, nsplit, part_stride,
+                                                        out, err);
     } else {
         allow_max_dynamic_smem(k_gram_tc<3>);
-        k_gram_tc<3><<<grid, 128, GtCfg<3>::SMEM, s>>>(map, map_lo, counts, poff, m, ld, nt, S, err);
+        k_gram_tc<3><<<grid, 128, GtCfg<3>::SMEM, s>>>(map, map_lo, counts, poff, m, ld, nt, nsplit, part_stride,
+                                                        out, err);
     }
     TC_CHECK_LAUNCH();
+    if (nsplit > 1) {
+        k_gram_sum<<<dim3(ceil_div((int64_t)m * ld / 4, 256 * 4), k), 256, 0, s>>>(out, nsplit, part_stride, counts,
+                                                                                  KE, m, ld, S);
+        TC_CHECK_LAUNCH();
+    }
 }
 
 }  // namespace tc
