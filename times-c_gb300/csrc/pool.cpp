@@ -180,9 +180,10 @@ uint64_t tc_job_footprint(const tc_job* j) {
     b += (k * m + k) * 8 + 3 * k * m * 4;  // row sums, power-iteration vectors
     b += k * 8 * 4;                        // counts, offsets, padded offsets, gates
     const uint64_t esize = j->precision == TC_PREC_BF16 ? 2 : 4;
+    const uint64_t planes = j->precision == TC_PREC_FP32 ? 2 : 1;
     const uint64_t mp64 = (m + 63) / 64 * 64;
     const uint64_t Psq = std::max<uint64_t>((k * mp64 + 63 * k + 63) / 64 * 64, 64);
-    b += std::max(m * Pp * esize, m * Psq * 4);  // Gram operand (members, or the squared matrices)
+    b += std::max(m * Pp * esize * planes, m * Psq * 8);  // Gram operand (members, or the squared matrices)
     const bool screened = j->precision == TC_PREC_FP32 && tc::screen_supported(j->m, (int)F, j->k);
     if ((j->precision != TC_PREC_FP32 && tc::tc_assign_supported(j->m, (int)F, j->k, j->precision)) || screened) {
         const uint64_t mp = (m + 63) / 64 * 64;
