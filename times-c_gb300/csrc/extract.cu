@@ -360,8 +360,8 @@ void extract_async(tc_ctx* ctx, const ExtractArgs& a, cudaStream_t s) {
     if (fused) {
         const GramOperand op = gram_tc_operand(ctx, n, k, m, a.precision);
         float* first = ws.first.as<float>((size_t)k * m);
-        launch_gather_norm_t(a.x, perm, a.labels, shift, gate, offsets, counts, k, poff, n, m, op.fmt, op.YT, op.Pp,
-                             first, s);
+        launch_gather_norm_t(a.x, perm, a.labels, shift, gate, offsets, counts, k, poff, n, m, op.fmt == 1, op.YT,
+                             op.YTlo, op.Pp, first, s);
         lead = first;
     } else {
         seg = ws.seg.as<float>((size_t)std::max<int64_t>(n, 1) * m);

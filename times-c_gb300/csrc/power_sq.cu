@@ -9,8 +9,7 @@
 //   P_0 = M / trace(M),  P_{j+1} = P_j^2 / trace(P_j^2),  v <- P_j v for bit j of e.
 // M is symmetric, so P_j^2 = P_j P_j^T is a Gram matrix: the 3xTF32 tensor-core
 // Gram kernel computes it with the rows of P_j as the "members" of cluster c
-// (P_j in FP32 in the transposed operand at columns poff[c] .. poff[c] + m; the
-// Gram kernel splits it into TF32 hi and lo parts).  The trace
+// (P_j in the transposed operand at columns poff[c] .. poff[c] + m).  The trace
 // normalisation keeps every P_j's largest eigenvalue in [1/m, 1], so nothing
 // overflows or underflows on the way.  The power-iteration kernel then starts
 // from the product, steps on until its convergence test passes, and applies the
@@ -29,6 +28,12 @@ namespace {
 constexpr int SQ_THREADS = 256;
 constexpr int SQ_ROWS = 32;  // rows of P per block
 
+__device__ __forceinline__ float tf32_round(float x) {
+    uint32_t r;
+    asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(r) : "f"(x));
+    return __uint_as_float(r);
+}
+
 __device__ __forceinline__ double sum_block_d(double v, double* red) {
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
@@ -41,12 +46,18 @@ __device__ __forceinline__ double sum_block_d(double v, double* red) {
     return s;
 }
 
-// P_0 = M / trace(M) into the operand; flags and padded offsets per cluster.
+__device__ __forceinline__ void put_split(float* YT, float* YTlo, int64_t idx, float x) {
+    const float hi = tf32_round(x);
+    YT[idx] = hi;
+    YTlo[idx] = tf32_round(x - hi);
+}
+
+// P_0 = M / trace(M) into the operand planes; flags and padded offsets per cluster.
 __global__ void __launch_bounds__(SQ_THREADS) k_sq_first(const float* __restrict__ S, int ld,
                                                          const double* __restrict__ r,
                                                          const double* __restrict__ tot,
                                                          const int32_t* __restrict__ counts, int m, int mp,
-                                                         int64_t Pp, float* __restrict__ YT,
+                                                         int64_t Pp, float* __restrict__ YT, float* __restrict__ YTlo,
                                                          int32_t* __restrict__ cnt_sq, int32_t* __restrict__ ok,
                                                          int64_t* __restrict__ poff) {
     __shared__ double red[SQ_THREADS / 32];
@@ -72,14 +83,14 @@ __global__ void __launch_bounds__(SQ_THREADS) k_sq_first(const float* __restrict
         const double ra = rc[a] * inv_m;
         for (int b = threadIdx.x; b < m; b += SQ_THREADS) {
             const double x = ((double)Sc[(size_t)a * ld + b] - ra - rc[b] * inv_m + tm) * inv;
-            YT[(int64_t)a * Pp + x0 + b] = (float)x;
+            put_split(YT, YTlo, (int64_t)a * Pp + x0 + b, (float)x);
         }
     }
 }
 
 // P_{j+1} = Q / trace(Q) with Q = P_j^2 from the Gram kernel.
 __global__ void __launch_bounds__(SQ_THREADS) k_sq_next(const float* __restrict__ Q, int ld, int m, int mp,
-                                                        int64_t Pp, float* __restrict__ YT,
+                                                        int64_t Pp, float* __restrict__ YT, float* __restrict__ YTlo,
                                                         int32_t* __restrict__ cnt_sq, int32_t* __restrict__ ok) {
     __shared__ double red[SQ_THREADS / 32];
     const int c = blockIdx.y;
@@ -100,12 +111,12 @@ __global__ void __launch_bounds__(SQ_THREADS) k_sq_next(const float* __restrict_
     const int a0 = blockIdx.x * SQ_ROWS, a1 = min(a0 + SQ_ROWS, m);
     for (int a = a0; a < a1; ++a)
         for (int b = threadIdx.x; b < m; b += SQ_THREADS)
-            YT[(int64_t)a * Pp + x0 + b] = Qc[(size_t)a * ld + b] * inv;
+            put_split(YT, YTlo, (int64_t)a * Pp + x0 + b, Qc[(size_t)a * ld + b] * inv);
 }
 
 // vout = P_j (vin / |vin|); vin == nullptr means v0 = [1, .5, 1, .5, ...].
-// Compensated FP32 sums per row.
-__global__ void __launch_bounds__(SQ_THREADS) k_sq_apply(const float* __restrict__ YT,
+// Compensated FP32 sums per row (the operand is hi + lo).
+__global__ void __launch_bounds__(SQ_THREADS) k_sq_apply(const float* __restrict__ YT, const float* __restrict__ YTlo,
                                                          int64_t Pp, int m, int mp, const int32_t* __restrict__ ok,
                                                          const float* __restrict__ vin, float* __restrict__ vout,
                                                          int ldv) {
@@ -126,9 +137,10 @@ __global__ void __launch_bounds__(SQ_THREADS) k_sq_apply(const float* __restrict
     const int a0 = blockIdx.x * SQ_ROWS, a1 = min(a0 + SQ_ROWS, m);
     for (int a = a0 + wid; a < a1; a += SQ_THREADS / 32) {
         const float* hr = YT + (int64_t)a * Pp + x0;
+        const float* lr = YTlo + (int64_t)a * Pp + x0;
         float s = 0.f, cp = 0.f;
         for (int b = lane; b < m; b += 32) {
-            const float pr = hr[b] * vs[b];
+            const float pr = (hr[b] + lr[b]) * vs[b];
             const float y = pr - cp, t = s + y;
             cp = (t - s) - y;
             s = t;
@@ -174,6 +186,7 @@ SquaringResult power_squaring(tc_ctx* ctx, const float* S, int ld, const double*
     const int64_t nsq = (int64_t)k * mp;  // operand columns: cluster c at c * mp
     const GramOperand op = gram_tc_operand(ctx, nsq, k, m, TC_PREC_FP32);
     float* YT = static_cast<float*>(op.YT);
+    float* YTlo = op.YTlo;
     float* Q = ws.gram_sq.as<float>((size_t)k * m * ld);
     float* vec = ws.piter.as<float>((size_t)2 * k * ld);
     char* meta = ws.sq_meta.as<char>((size_t)k * 16);
@@ -181,7 +194,7 @@ SquaringResult power_squaring(tc_ctx* ctx, const float* S, int ld, const double*
     int32_t* cnt_sq = reinterpret_cast<int32_t*>(meta + (size_t)k * 8);
     int32_t* ok = cnt_sq + k;
     const dim3 grid(ceil_div(m, SQ_ROWS), k);
-    k_sq_first<<<grid, SQ_THREADS, 0, s>>>(S, ld, r, tot, counts, m, mp, op.Pp, YT, cnt_sq, ok, poff);
+    k_sq_first<<<grid, SQ_THREADS, 0, s>>>(S, ld, r, tot, counts, m, mp, op.Pp, YT, YTlo, cnt_sq, ok, poff);
     TC_CHECK_LAUNCH();
     int J = 0;
     while ((e >> (J + 1)) > 0) ++J;
@@ -190,14 +203,14 @@ SquaringResult power_squaring(tc_ctx* ctx, const float* S, int ld, const double*
     for (int j = 0; j <= J; ++j) {
         if ((e >> j) & 1) {
             float* vout = vec + (size_t)cur * k * ld;
-            k_sq_apply<<<grid, SQ_THREADS, (size_t)m * sizeof(float), s>>>(YT, op.Pp, m, mp, ok, vin, vout, ld);
+            k_sq_apply<<<grid, SQ_THREADS, (size_t)m * sizeof(float), s>>>(YT, YTlo, op.Pp, m, mp, ok, vin, vout, ld);
             TC_CHECK_LAUNCH();
             vin = vout;
             cur ^= 1;
         }
         if (j < J) {
             launch_gram_tc(ctx, nullptr, cnt_sq, nullptr, poff, nsq, k, m, ld, TC_PREC_FP32, Q, err, s);
-            k_sq_next<<<grid, SQ_THREADS, 0, s>>>(Q, ld, m, mp, op.Pp, YT, cnt_sq, ok);
+            k_sq_next<<<grid, SQ_THREADS, 0, s>>>(Q, ld, m, mp, op.Pp, YT, YTlo, cnt_sq, ok);
             TC_CHECK_LAUNCH();
         }
     }

@@ -227,6 +227,7 @@ int run_extract(tc_ctx* ctx, const ExtractArgs& a, cudaStream_t s);
 // operand of the tensor-core Gram (transposed, cluster-padded members)
 struct GramOperand {
     void* YT = nullptr;
+    float* YTlo = nullptr;  // 3xTF32 lo plane
     int64_t Pp = 0;         // columns (padded positions)
     int fmt = 0;            // 1 BF16, 2 TF32, 3 3xTF32
 };
@@ -252,7 +253,7 @@ SquaringResult power_squaring(tc_ctx* ctx, const float* S, int ld, const double*
 bool gather_transposed_supported(int m);
 void launch_gather_norm_t(const float* x, const int32_t* perm, const int32_t* labels, const int32_t* shift,
                           const uint8_t* gate, const int32_t* offsets, const int32_t* counts, int k,
-                          const int64_t* poff, int64_t n, int m, int fmt, void* YT, int64_t Pp,
+                          const int64_t* poff, int64_t n, int m, bool bf16, void* YT, float* YTlo, int64_t Pp,
                           float* first, cudaStream_t s);
 
 // workspace of a context: free every buffer (the context must be idle) / bytes held

@@ -87,12 +87,11 @@ template <>
 __device__ __forceinline__ float convert_out<float>(float v) { return to_tf32(v); }
 
 // YT[a][p'] = seg[pos][a], p' = pos - offsets[c] + poff[c] for the cluster c holding pos.
-// raw (3xTF32 form): the FP32 value as it is (the Gram kernel splits it); else rounded
-// to the operand type.
+// With YTlo (3xTF32): YT gets tf32(x) and YTlo gets tf32(x - tf32(x)).
 template <class TO>
 __global__ void k_seg_transpose(const float* __restrict__ seg, int64_t n, int m, const int32_t* __restrict__ offsets,
                                 const int32_t* __restrict__ counts, const int64_t* __restrict__ poff, int k,
-                                TO* __restrict__ YT, int raw, int64_t Pp) {
+                                TO* __restrict__ YT, float* __restrict__ YTlo, int64_t Pp) {
     __shared__ float tile[32][33];
     const int tx = threadIdx.x, ty = threadIdx.y;
     const int64_t pos0 = (int64_t)blockIdx.x * 32;
@@ -119,7 +118,9 @@ __global__ void k_seg_transpose(const float* __restrict__ seg, int64_t n, int m,
         const int a = a0 + ty + 8 * i;
         if (a < m) {
             const float x = tile[tx][ty + 8 * i];
-            YT[(int64_t)a * Pp + pp] = raw ? TO(x) : convert_out<TO>(x);
+            const TO hi = convert_out<TO>(x);
+            YT[(int64_t)a * Pp + pp] = hi;
+            if (YTlo) YTlo[(int64_t)a * Pp + pp] = to_tf32(x - (float)hi);
         }
     }
 }
@@ -127,14 +128,14 @@ __global__ void k_seg_transpose(const float* __restrict__ seg, int64_t n, int m,
 // ---------------------------------------------------------------- Gram kernel
 template <int FMT>
 __global__ void __launch_bounds__(128, 1) k_gram_tc(const __grid_constant__ CUtensorMap tmap,
+                                                    const __grid_constant__ CUtensorMap tmap_lo,
                                                     const int32_t* __restrict__ counts,
                                                     const int64_t* __restrict__ poff, int m, int ld, int nt,
                                                     int nsplit, size_t part_stride, float* __restrict__ S,
                                                     int* __restrict__ err) {
     extern __shared__ uint8_t smem_raw[];
     typedef GtCfg<FMT> G;
-    // full: the stage's tiles landed; conv (3xTF32): split into hi | lo; empty: MMAs done
-    __shared__ __align__(8) uint64_t full[G::STAGES], conv[G::STAGES], empty[G::STAGES], done;
+    __shared__ __align__(8) uint64_t full[G::STAGES], empty[G::STAGES], done;
     __shared__ uint32_t tmem_base;
     uint8_t* base = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
     const int c = blockIdx.y;
@@ -152,12 +153,12 @@ __global__ void __launch_bounds__(128, 1) k_gram_tc(const __grid_constant__ CUte
     if (threadIdx.x == 0) {
         for (int s = 0; s < G::STAGES; ++s) {
             sm100::mbar_init(&full[s], 1);
-            sm100::mbar_init(&conv[s], 2);  // one arrival per converting warp
             sm100::mbar_init(&empty[s], 1);
         }
         sm100::mbar_init(&done, 1);
         sm100::fence_mbar_init();
         sm100::prefetch_tmap(&tmap);
+        if (FMT == 3) sm100::prefetch_tmap(&tmap_lo);
     }
     if (warp == 0) {
         sm100::tmem_alloc(&tmem_base, 128);
@@ -177,10 +178,14 @@ __global__ void __launch_bounds__(128, 1) k_gram_tc(const __grid_constant__ CUte
             if (!ok) break;
             uint8_t* A = base + (size_t)s * G::TILES * GT_TILE_BYTES;  // [A | B | A_lo | B_lo]
             // a diagonal tile's B is its A: loaded once
-            sm100::mbar_expect_tx(&full[s], (ta == tb ? 1 : 2) * GT_TILE_BYTES);
+            sm100::mbar_expect_tx(&full[s], (ta == tb ? G::TILES / 2 : G::TILES) * GT_TILE_BYTES);
             const int xk = x0 + (kb0 + kb) * KE;
             sm100::tma_load_2d(A, &tmap, xk, ta * GT_TILE, &full[s]);
             if (ta != tb) sm100::tma_load_2d(A + GT_TILE_BYTES, &tmap, xk, tb * GT_TILE, &full[s]);
+            if (FMT == 3) {
+                sm100::tma_load_2d(A + 2 * GT_TILE_BYTES, &tmap_lo, xk, ta * GT_TILE, &full[s]);
+                if (ta != tb) sm100::tma_load_2d(A + 3 * GT_TILE_BYTES, &tmap_lo, xk, tb * GT_TILE, &full[s]);
+            }
         }
         // the MMA thread's last commits to empty[] arrive when their MMAs end: wait for
         // them, so no arrival lands in this CTA's shared memory after it has left
@@ -193,7 +198,7 @@ __global__ void __launch_bounds__(128, 1) k_gram_tc(const __grid_constant__ CUte
         constexpr uint32_t ID = sm100::idesc(FMT == 1 ? 1 : 2, 128, 128);
         for (int kb = 0; kb < nk && ok; ++kb) {
             const int s = kb % G::STAGES, u = kb / G::STAGES;
-            ok = sm100::mbar_wait(FMT == 3 ? &conv[s] : &full[s], u & 1, err);
+            ok = sm100::mbar_wait(&full[s], u & 1, err);
             if (!ok) break;
             sm100::tc_fence_after();
             uint8_t* A = base + (size_t)s * G::TILES * GT_TILE_BYTES;
@@ -216,33 +221,6 @@ __global__ void __launch_bounds__(128, 1) k_gram_tc(const __grid_constant__ CUte
             sm100::mma_commit(&empty[s]);
         }
         sm100::mma_commit(&done);
-    } else if (FMT == 3 && warp >= 2) {
-        // converters: each landed FP32 tile becomes its TF32 hi part in place and its lo
-        // part x - tf32(x), rounded to TF32, in the lo slot (elementwise at the same
-        // offsets, so the 128-byte swizzle carries over); then a proxy fence makes the
-        // writes visible to the tensor cores before the stage is handed on
-        const int ct = (warp - 2) * 32 + lane;  // 0..63
-        for (int kb = 0; kb < nk && ok; ++kb) {
-            const int s = kb % G::STAGES, u = kb / G::STAGES;
-            ok = __all_sync(0xffffffffu, sm100::mbar_wait(&full[s], u & 1, err));
-            if (!ok) break;
-            uint8_t* A = base + (size_t)s * G::TILES * GT_TILE_BYTES;
-            for (int tile = 0; tile < (ta == tb ? 1 : 2); ++tile) {
-                float4* hi = reinterpret_cast<float4*>(A + tile * GT_TILE_BYTES);
-                float4* lo = reinterpret_cast<float4*>(A + (2 + tile) * GT_TILE_BYTES);
-#pragma unroll 4
-                for (int e = ct; e < GT_TILE_BYTES / 16; e += 64) {
-                    const float4 v = hi[e];
-                    const float4 h = make_float4(to_tf32(v.x), to_tf32(v.y), to_tf32(v.z), to_tf32(v.w));
-                    lo[e] = make_float4(to_tf32(v.x - h.x), to_tf32(v.y - h.y), to_tf32(v.z - h.z),
-                                        to_tf32(v.w - h.w));
-                    hi[e] = h;
-                }
-            }
-            sm100::fence_proxy_async();
-            __syncwarp();
-            if (lane == 0) sm100::mbar_arrive(&conv[s]);
-        }
     }
     __syncwarp();
     // epilogue: warp w owns TMEM lanes 32w..32w+31 = rows a0 + 32w + lane
@@ -313,7 +291,7 @@ bool gram_tc_supported(int m, int precision) {
 // Zero the padding columns of cluster c: [poff + count, poff + roundup(count, 64)), every row.
 template <class TO>
 __global__ void k_zero_pads(const int32_t* __restrict__ counts, const int64_t* __restrict__ poff, int m, int64_t Pp,
-                            TO* __restrict__ YT) {
+                            TO* __restrict__ YT, float* __restrict__ YTlo) {
     const int c = blockIdx.x;
     const int cnt = counts[c];
     const int pad = (cnt + GT_PAD - 1) / GT_PAD * GT_PAD - cnt;
@@ -321,6 +299,7 @@ __global__ void k_zero_pads(const int32_t* __restrict__ counts, const int64_t* _
     for (int e = threadIdx.x; e < pad * m; e += blockDim.x) {
         const int a = e / pad, q = e % pad;
         YT[(int64_t)a * Pp + c0 + q] = TO(0.f);
+        if (YTlo) YTlo[(int64_t)a * Pp + c0 + q] = 0.f;
     }
 }
 
@@ -332,18 +311,21 @@ int64_t gram_padded_cols(int64_t n, int k) {
 }
 
 // The transposed, cluster-padded operand of the tensor-core Gram in the workspace:
-// BF16 (precision BF16), TF32 (TF32), or FP32 (3xTF32: the Gram kernel splits it into TF32 hi and
-// lo parts in shared memory).
+// BF16 (precision BF16), TF32 (TF32), or TF32 hi and lo planes (FP32: 3xTF32).
 size_t gram_operand_bytes(int64_t n, int k, int m, int precision) {
     const int fmt = precision == TC_PREC_BF16 ? 1 : (precision == TC_PREC_TF32 ? 2 : 3);
-    return (size_t)m * gram_padded_cols(n, k) * (fmt == 1 ? 2 : 4);
+    return (size_t)m * gram_padded_cols(n, k) * (fmt == 1 ? 2 : 4) * (fmt == 3 ? 2 : 1);
 }
 
 GramOperand gram_tc_operand(tc_ctx* ctx, int64_t n, int k, int m, int precision) {
     GramOperand o;
     o.Pp = gram_padded_cols(n, k);
     o.fmt = precision == TC_PREC_BF16 ? 1 : (precision == TC_PREC_TF32 ? 2 : 3);
-    o.YT = ctx->ws.gram_yt.get(gram_operand_bytes(n, k, m, precision));
+    const int esize = o.fmt == 1 ? 2 : 4;
+    const size_t plane = (size_t)m * o.Pp * esize;
+    char* YT = static_cast<char*>(ctx->ws.gram_yt.get(gram_operand_bytes(n, k, m, precision)));
+    o.YT = YT;
+    o.YTlo = o.fmt == 3 ? reinterpret_cast<float*>(YT + plane) : nullptr;
     return o;
 }
 
@@ -357,24 +339,25 @@ void launch_gram_tc(tc_ctx* ctx, const float* seg, const int32_t* counts, const 
     const int fmt = op.fmt;
     const int esize = fmt == 1 ? 2 : 4;
     char* YT = static_cast<char*>(op.YT);
+    float* YTlo = op.YTlo;
     // only the padding needs zeros: the transpose writes every member column
     if (fmt == 1)
-        k_zero_pads<__nv_bfloat16><<<k, 256, 0, s>>>(counts, poff, m, Pp, (__nv_bfloat16*)YT);
+        k_zero_pads<__nv_bfloat16><<<k, 256, 0, s>>>(counts, poff, m, Pp, (__nv_bfloat16*)YT, nullptr);
     else
-        k_zero_pads<float><<<k, 256, 0, s>>>(counts, poff, m, Pp, (float*)YT);
+        k_zero_pads<float><<<k, 256, 0, s>>>(counts, poff, m, Pp, (float*)YT, YTlo);
     TC_CHECK_LAUNCH();
     dim3 tg(ceil_div(n, 32), ceil_div(m, 32)), tb(32, 8);
     if (n > 0 && seg) {
         if (fmt == 1)
             k_seg_transpose<__nv_bfloat16><<<tg, tb, 0, s>>>(seg, n, m, offsets, counts, poff, k,
-                                                             (__nv_bfloat16*)YT, 0, Pp);
+                                                             (__nv_bfloat16*)YT, nullptr, Pp);
         else
-            k_seg_transpose<float><<<tg, tb, 0, s>>>(seg, n, m, offsets, counts, poff, k, (float*)YT,
-                                                     fmt == 3 ? 1 : 0, Pp);
+            k_seg_transpose<float><<<tg, tb, 0, s>>>(seg, n, m, offsets, counts, poff, k, (float*)YT, YTlo, Pp);
         TC_CHECK_LAUNCH();
     }
     const CUtensorMapDataType dt = fmt == 1 ? CU_TENSOR_MAP_DATA_TYPE_BFLOAT16 : CU_TENSOR_MAP_DATA_TYPE_FLOAT32;
     CUtensorMap map = make_tmap_2d(YT, dt, esize, (uint64_t)m, (uint64_t)Pp, GT_TILE);
+    CUtensorMap map_lo = fmt == 3 ? make_tmap_2d(YTlo, dt, esize, (uint64_t)m, (uint64_t)Pp, GT_TILE) : map;
     const int nt = ceil_div(m, GT_TILE);
     // K split across CTAs so the launch fills its last wave (one CTA per SM: the
     // operand ring takes most of the shared memory): the share count with the best
@@ -395,15 +378,15 @@ void launch_gram_tc(tc_ctx* ctx, const float* seg, const int32_t* counts, const 
     dim3 grid(nt * (nt + 1) / 2, k, nsplit);
     if (fmt == 1) {
         allow_max_dynamic_smem(k_gram_tc<1>);
-        k_gram_tc<1><<<grid, 128, GtCfg<1>::SMEM, s>>>(map, counts, poff, m, ld, nt, nsplit, part_stride,
+        k_gram_tc<1><<<grid, 128, GtCfg<1>::SMEM, s>>>(map, map_lo, counts, poff, m, ld, nt, nsplit, part_stride,
                                                         out, err);
     } else if (fmt == 2) {
         allow_max_dynamic_smem(k_gram_tc<2>);
-        k_gram_tc<2><<<grid, 128, GtCfg<2>::SMEM, s>>>(map, counts, poff, m, ld, nt, nsplit, part_stride,
+        k_gram_tc<2><<<grid, 128, GtCfg<2>::SMEM, s>>>(map, map_lo, counts, poff, m, ld, nt, nsplit, part_stride,
                                                         out, err);
     } else {
         allow_max_dynamic_smem(k_gram_tc<3>);
-        k_gram_tc<3><<<grid, 128, GtCfg<3>::SMEM, s>>>(map, counts, poff, m, ld, nt, nsplit, part_stride,
+        k_gram_tc<3><<<grid, 128, GtCfg<3>::SMEM, s>>>(map, map_lo, counts, poff, m, ld, nt, nsplit, part_stride,
                                                         out, err);
     }
     TC_CHECK_LAUNCH();

@@ -214,9 +214,8 @@ __device__ __forceinline__ float to_operand<float>(float v) {  // TF32 rounding 
 // transposed into the tensor-core Gram's operand YT[a][pp] (pp: the position in
 // the cluster-padded layout) instead of row-major: the row-major copy and the
 // separate transpose pass are never made.  The first member of each cluster also
-// goes to first[c][*] (the sign rule's reference row).  FP32 operands are written
-// rounded to TF32 (TF32 form) or as they are (3xTF32 form: the Gram kernel splits
-// them into TF32 hi and lo parts in shared memory).  Rows are staged in shared memory with
+// goes to first[c][*] (the sign rule's reference row).  With YTlo (3xTF32) the lo
+// plane gets x - tf32(x) rounded to TF32.  Rows are staged in shared memory with
 // pitch m+1 so the transposed reads are free of bank conflicts.
 template <int VPL, class TO>
 __global__ void __launch_bounds__(256) k_gather_norm_t(const float* __restrict__ src, int64_t n, int m,
@@ -227,7 +226,7 @@ __global__ void __launch_bounds__(256) k_gather_norm_t(const float* __restrict__
                                                        const int32_t* __restrict__ offsets,
                                                        const int32_t* __restrict__ counts, int k,
                                                        const int64_t* __restrict__ poff, TO* __restrict__ YT,
-                                                       int raw, int64_t Pp,
+                                                       float* __restrict__ YTlo, int64_t Pp,
                                                        float* __restrict__ first) {
     extern __shared__ float tile[];  // [32][m + 1]
     const int pitch = m + 1;
@@ -282,7 +281,9 @@ __global__ void __launch_bounds__(256) k_gather_norm_t(const float* __restrict__
     const int64_t pp = pos - offsets[c] + poff[c];
     for (int a = wid; a < m; a += 8) {
         const float y = tile[r * pitch + a];
-        YT[(int64_t)a * Pp + pp] = raw ? TO(y) : to_operand<TO>(y);
+        const TO hi = to_operand<TO>(y);
+        YT[(int64_t)a * Pp + pp] = hi;
+        if (YTlo) YTlo[(int64_t)a * Pp + pp] = to_operand<float>(y - (float)hi);
     }
 }
 
@@ -290,7 +291,7 @@ bool gather_transposed_supported(int m) { return m >= 2 && m <= 1024; }
 
 void launch_gather_norm_t(const float* x, const int32_t* perm, const int32_t* labels, const int32_t* shift,
                           const uint8_t* gate, const int32_t* offsets, const int32_t* counts, int k,
-                          const int64_t* poff, int64_t n, int m, int fmt, void* YT, int64_t Pp,
+                          const int64_t* poff, int64_t n, int m, bool bf16, void* YT, float* YTlo, int64_t Pp,
                           float* first, cudaStream_t s) {
     if (n == 0) return;
     TC_REQUIRE(gather_transposed_supported(m), TC_ERR_UNSUPPORTED, "fused gather: m must be in [2, 1024]");
@@ -298,16 +299,16 @@ void launch_gather_norm_t(const float* x, const int32_t* perm, const int32_t* la
     const int grid = ceil_div(n, 32);
 #define GT(VPL)                                                                                                 \
     do {                                                                                                        \
-        if (fmt == 1) {                                                                                         \
+        if (bf16) {                                                                                             \
             allow_max_dynamic_smem(k_gather_norm_t<VPL, __nv_bfloat16>);                                        \
             k_gather_norm_t<VPL, __nv_bfloat16><<<grid, 256, smem, s>>>(x, n, m, perm, labels, shift, gate,     \
                                                                         offsets, counts, k, poff,               \
-                                                                        (__nv_bfloat16*)YT, 0, Pp, first);     \
+                                                                        (__nv_bfloat16*)YT,                     \
+                                                                        nullptr, Pp, first);                   \
         } else {                                                                                                \
             allow_max_dynamic_smem(k_gather_norm_t<VPL, float>);                                                \
             k_gather_norm_t<VPL, float><<<grid, 256, smem, s>>>(x, n, m, perm, labels, shift, gate, offsets,    \
-                                                                counts, k, poff, (float*)YT, fmt == 3 ? 1 : 0,  \
-                                                                Pp, first);                                     \
+                                                                counts, k, poff, (float*)YT, YTlo, Pp, first);  \
         }                                                                                                       \
     } while (0)
     if (m <= 64) GT(2);
