@@ -2,10 +2,11 @@
 order) against the unsplit launch (TIMESC_GRAM_NOSPLIT) and the FP64 oracle.
 
 The split is chosen from the launch's wave occupancy when every share keeps at least
-32 K blocks on average: m = 512, k = 4, n = 12000 takes 2 shares, m = 300, k = 3,
-n = 20000 takes 4.  A different summation order moves the Gram by rounding only:
-centroids within 2e-5 (3xTF32) / 1e-4 (BF16) of the unsplit ones, and the FP32 form
-within 1e-4 of the oracle.
+128 K blocks on average: both cases (m = 512, k = 2, n = 40000 and m = 300, k = 3,
+n = 60000) take 4 shares in FP32 (32-member blocks) and 2 in BF16 (64-member blocks).
+A different summation order moves the Gram by rounding only: centroids within 2e-5
+(3xTF32) / 1e-4 (BF16) of the unsplit ones, and the FP32 form within 1e-4 of the
+oracle.
 """
 import numpy as np
 import pytest
@@ -31,7 +32,7 @@ def _extract(ctx, X, labels, k, prec, monkeypatch, split):
     return sc, c.cpu().numpy()
 
 
-@pytest.mark.parametrize("m,k,n", [(512, 4, 12000), (300, 3, 20000)])
+@pytest.mark.parametrize("m,k,n", [(512, 2, 40000), (300, 3, 60000)])
 @pytest.mark.parametrize("prec,tol", [(0, 2e-5), (1, 1e-4)])
 def test_split_gram_matches_unsplit_and_oracle(gpu_ctx, built, monkeypatch, m, k, n, prec, tol):
     T, O = built

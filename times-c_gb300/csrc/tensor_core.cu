@@ -361,7 +361,9 @@ void launch_gram_tc(tc_ctx* ctx, const float* seg, const int32_t* counts, const 
     const int nt = ceil_div(m, GT_TILE);
     // K split across CTAs so the launch fills its last wave (one CTA per SM: the
     // operand ring takes most of the shared memory): the share count with the best
-    // wave occupancy, each share keeping at least 32 K blocks on average
+    // wave occupancy, each share keeping at least 128 K blocks on average (with fewer,
+    // a CTA's fixed costs - setup, pipeline fill, the tile and mirror stores, its
+    // partial's share of the sum - outweigh the fuller wave)
     const int KE = fmt == 1 ? GtCfg<1>::KE : GtCfg<3>::KE;
     const int units = nt * (nt + 1) / 2 * k;
     const int64_t avg_kb = std::max<int64_t>(1, n / std::max(k, 1) / KE);
@@ -370,7 +372,7 @@ void launch_gram_tc(tc_ctx* ctx, const float* seg, const int32_t* counts, const 
         return x / std::ceil(x);
     };
     int nsplit = 1;
-    for (int sp = 2; sp <= 4 && avg_kb / sp >= 32; ++sp)
+    for (int sp = 2; sp <= 4 && avg_kb / sp >= 128; ++sp)
         if (occupancy(sp) > occupancy(nsplit) + 0.02) nsplit = sp;
     if (std::getenv("TIMESC_GRAM_NOSPLIT")) nsplit = 1;
     const size_t part_stride = (size_t)k * m * ld;
