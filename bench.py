@@ -1,7 +1,7 @@
 """k-Shape benchmark on GB300.
 
-Workload (default): the precision configuration of the Times-C baseline,
-n = 1,000,000 series, m = 512, k = 32, synthetic data (the prototype generator
+Workload (default): the precision workload, n = 1,000,000 series, m = 512,
+k = 32, synthetic data (the prototype generator
 of times-c_gb300/csrc/gen.cpp, noise 0.3), in the mixed-precision form (BF16
 tensor-core correlation and Gram, FP32 accumulation); the plain FP32 form runs
 beside it on the same series and the line reports both and how far apart their
@@ -14,8 +14,9 @@ with the series resident in HBM.
              (host->device copy of the series, z-norm, loop, labels and
              centroids back), pairs/s = n*k*iterations / wall time
   roofline   the dominant kernel (the fused SBD assignment), CUDA events on
-             the launching stream; algorithmic work per launch as documented
-             in DESIGN.md
+             the launching stream; algorithmic work per launch: 2*n*k*F*m
+             flops for the tensor-core correlation (m products per lag, F
+             lags), the FFT flop count of fft_flops() for the FP32 kernel
   cpu_baseline  the FP64 oracle (a restatement, "port") on the host cores,
              one iteration on a bounded sample of the same workload
 
