@@ -36,7 +36,7 @@ bool parse_line(const Line& L, bool labeled, std::vector<float>& vals, int32_t& 
     const char* p = L.b;
     const char* e = L.e;
     while (e > p && is_ws(e[-1])) --e;
-    bool comma = std::memchr(p, ',', (size_t)(e - p)) != nullptr;
+    const bool comma = e > p && std::memchr(p, ',', (size_t)(e - p)) != nullptr;
     std::vector<std::pair<const char*, const char*>> fields;
     if (comma) {
         const char* s = p;
