@@ -164,3 +164,56 @@ def test_job_footprint_estimate(built):
     assert fp(0, 512, 8) == 0 and fp(100, 1, 8) == 0
     # the serving form's large request (n=2e5, m=1024, k=16) stays in the single-digit GB
     assert 2e9 < fp(200000, 1024, 16) < 1e10
+
+
+def _load_bench():
+    import importlib.util
+    import sys
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    spec = importlib.util.spec_from_file_location("bench_under_test", os.path.join(root, "bench.py"))
+    b = importlib.util.module_from_spec(spec)
+    argv = sys.argv
+    sys.argv = ["bench.py"]
+    try:
+        spec.loader.exec_module(b)
+    finally:
+        sys.argv = argv
+    return b
+
+
+def test_bench_clock_window(tmp_path):
+    """bench.py's clock record keeps only the nvidia-smi samples taken inside the timed
+    region (with 25 ms of slack), collects the throttle reasons seen there, and falls
+    back to every sample, saying so, when none landed inside."""
+    import datetime
+    import tempfile
+    b = _load_bench()
+
+    class FakeProc:
+        def terminate(self):
+            pass
+
+        def wait(self):
+            pass
+
+    def clocks_with(samples, t0, t1):
+        c = b.Clocks.__new__(b.Clocks)
+        c.f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False, dir=tmp_path)
+        for ts, mhz, cap in samples:
+            c.f.write("%s, %d, 2070, 900.0, Not Active, Not Active, Not Active, %s\n"
+                      % (ts.strftime("%Y/%m/%d %H:%M:%S.%f")[:-3], mhz, "Active" if cap else "Not Active"))
+        c.f.flush()
+        c.p = FakeProc()
+        c.t0, c.t1 = t0, t1
+        return c.stop()
+
+    now = datetime.datetime(2026, 1, 1, 12, 0, 0)
+    ms = lambda x: now + datetime.timedelta(milliseconds=x)
+    samples = [(ms(0), 1000, False), (ms(100), 2070, False), (ms(120), 2070, True), (ms(140), 2070, False),
+               (ms(400), 1200, False)]
+    r = clocks_with(samples, ms(90), ms(150))
+    assert r["samples"] == 3 and r["sm_mhz"] == 2070.0
+    assert r["reasons"] == ["sw_power_cap"]
+    assert r["window"].startswith("timed region")
+    r = clocks_with(samples, ms(200), ms(300))  # nothing inside: all samples, flagged
+    assert r["samples"] == 5 and r["window"].startswith("no sample inside")
