@@ -244,6 +244,18 @@ def host_threads():
         return os.cpu_count() or 1
 
 
+def max_over_ranks(value, dist):
+    """The largest of every rank's value (the slowest replica's time), on all ranks:
+    a GPU tensor under NCCL, a host tensor under gloo."""
+    import torch
+    if dist is None:
+        return value
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([float(value)], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return t.item()
+
+
 def run_reference(args, wl):
     """The reference's CPU implementation of the path (FP64 port), rank 0 only."""
     rank = int(os.environ.get("RANK", "0"))
@@ -617,11 +629,8 @@ def main():
     ms = t_start.elapsed_time(t_end)
     assign_ms = [a.elapsed_time(b) for a, b in ev]
     if dist:
-        t = torch.tensor([ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = t.item()
-        if dist:
-            dist.barrier()
+        ms = max_over_ranks(ms, dist)
+        dist.barrier()
     ms_step = ms / args.steps
     value = world * n * k / (ms_step / 1e3)
     a_ms = statistics.mean(assign_ms)
