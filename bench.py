@@ -146,7 +146,10 @@ class Clocks:
         self.p.wait()
         self.f.flush()
         rows = []
-        for line in open(self.f.name):
+        self.f.close()
+        with open(self.f.name) as fh:
+            lines = fh.readlines()
+        for line in lines:
             parts = [t.strip() for t in line.split(",")]
             if len(parts) != 8:
                 continue

@@ -17,7 +17,8 @@ def T(built):
 
 
 def header_symbols():
-    text = open(os.path.join(ROOT, "include", "timesc.h")).read()
+    with open(os.path.join(ROOT, "include", "timesc.h")) as f:
+        text = f.read()
     return sorted(set(re.findall(r"^\s*(?:int|void|uint64_t|const char\s*\*)\s+(tc_[a-z_0-9]+)\s*\(", text, re.M)))
 
 
@@ -81,7 +82,8 @@ def test_parser_errors(T, tmp_path):
 def test_label_writer_matches_reference(T, golden, tmp_path):
     p = str(tmp_path / "labels.txt")
     T.write_labels(p, np.array([1, 2, 10, 3, -1]))
-    assert open(p, "rb").read() == bytes(golden["writefile"])
+    with open(p, "rb") as f:
+        assert f.read() == bytes(golden["writefile"])
 
 
 def test_centroid_writer_roundtrip(T, tmp_path):

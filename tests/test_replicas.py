@@ -41,7 +41,7 @@ def _rank_main(rank, world, port, values, out):
 def test_max_over_ranks_gloo_world_2():
     import torch.multiprocessing as mp
     port = _free_port()
-    mgr = mp.Manager()
+    mgr = mp.get_context("spawn").Manager()  # no fork of a process that may hold CUDA state
     out = mgr.dict()
     mp.spawn(_rank_main, args=(2, port, [12.5, 31.25], out), nprocs=2, join=True)
     assert out[0] == out[1] == 31.25
