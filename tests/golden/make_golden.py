@@ -1,7 +1,7 @@
 """Generates tests/golden/reference_golden.npz from the reference's own code.
 
-Run here, where the Times-C tree is mounted (default /root/reference; override
-with TIMESC_REFERENCE):  python tests/golden/make_golden.py
+Run where the Times-C tree is present (TIMESC_REFERENCE, else the directory
+`reference` beside the repository):  python tests/golden/make_golden.py
 
 * Code/test/test_timesC.py is imported (numpy >= 2 removed np.Inf, which it
   uses: the alias is restored before import).  Its functions are run on seeded
@@ -27,7 +27,7 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(os.path.dirname(HERE))
-REF = os.environ.get("TIMESC_REFERENCE", "/root/reference")
+REF = os.environ.get("TIMESC_REFERENCE", os.path.join(os.path.dirname(ROOT), "reference"))
 sys.path.insert(0, os.path.join(ROOT, "times-c_gb300"))
 import timesc  # noqa: E402
 

@@ -76,6 +76,9 @@ static void assign(tc_ctx* ctx, const float* x, const float* C, int64_t n, int m
         a.centroids = C;
         a.cand = ctx->ws.screen.as<int32_t>((size_t)n * (SCREEN_CAP + 1));
         a.ncand = a.cand + (size_t)n * SCREEN_CAP;
+        // -1 (all centroids) for every series the tensor-core pass does not reach,
+        // e.g. after one of its bounded waits ran out
+        TC_CUDA(cudaMemsetAsync(a.ncand, 0xFF, (size_t)n * sizeof(int32_t), s));
         launch_assign_tc(ctx, a, TC_PREC_BF16, s);
         float2* spec = ctx->ws.spectra.as<float2>((size_t)k * (F / 2 + 1));
         launch_centroid_spectra(ctx, C, k, m, F, spec, s);

@@ -23,24 +23,36 @@ using namespace tcfft;
 namespace tc {
 
 // ------------------------------------------------------------------ tables
+// twN[e] = exp(-2 pi i e/N), twF[e] = exp(-2 pi i e/(2N)), e in [0, N), from the
+// FP64 sincospi rounded to float.  The context's tables and the allocation-free
+// entry point's both come from this kernel, so the two paths transform with
+// identical twiddles.
+__global__ void k_twiddles(float2* twN, float2* twF, int N) {
+    const int e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e < N) {
+        double s, c;
+        sincospi(-2.0 * (double)e / (double)N, &s, &c);
+        twN[e] = make_float2((float)c, (float)s);
+        sincospi(-(double)e / (double)N, &s, &c);
+        twF[e] = make_float2((float)c, (float)s);
+    }
+}
+
 const FftTables& fft_tables(tc_ctx* ctx, int F) {
     for (auto* t : ctx->fft)
         if (t->F == F) return *t;
     auto* t = new FftTables();
     t->F = F;
-    int N = F / 2;
-    std::vector<float2> hN(N), hF(N);
-    for (int e = 0; e < N; ++e) {
-        double a = -2.0 * M_PI * (double)e / (double)N;
-        double b = -2.0 * M_PI * (double)e / (double)F;
-        hN[e] = make_float2((float)std::cos(a), (float)std::sin(a));
-        hF[e] = make_float2((float)std::cos(b), (float)std::sin(b));
-    }
-    std::lock_guard<std::recursive_mutex> lk(capture_mutex());  // synchronous copies: not while another thread captures
+    const int N = F / 2;
+    // built once per context and length, finished before the first use on any
+    // stream (the legacy stream, as a synchronous copy would be; not while
+    // another thread captures a graph)
+    std::lock_guard<std::recursive_mutex> lk(capture_mutex());
     float2* dN = t->twN.as<float2>(N);
     float2* dF = t->twF.as<float2>(N);
-    TC_CUDA(cudaMemcpy(dN, hN.data(), sizeof(float2) * N, cudaMemcpyHostToDevice));
-    TC_CUDA(cudaMemcpy(dF, hF.data(), sizeof(float2) * N, cudaMemcpyHostToDevice));
+    k_twiddles<<<ceil_div(N, 256), 256, 0, 0>>>(dN, dF, N);
+    TC_CHECK_LAUNCH();
+    TC_CUDA(cudaStreamSynchronize(0));
     ctx->fft.push_back(t);
     return *t;
 }
@@ -284,8 +296,8 @@ __global__ void __launch_bounds__(Cfg<N>::BLOCK, 1) k_assign_fft(AssignParams p)
         const int32_t* cl = nullptr;
         int ncl = -1;
         if (p.cand) {
-            ncl = p.ncand[i];
             cl = p.cand + (size_t)i * SCREEN_CAP;
+            ncl = screen_list_len(cl, p.ncand[i], p.k);
         }
         const int iters = ncl >= 0 ? ncl : c1 - c0;
         float bestd = 1e10f;  // get_pos_idx: min_val = 1e10, pos = 0
@@ -558,25 +570,13 @@ static NoallocDevice noalloc_setup(int dev) {
     return d;
 }
 
-// twN[e] = exp(-2 pi i e/N), twF[e] = exp(-2 pi i e/(2N)), e in [0, N)
-__global__ void k_noalloc_twiddles(float2* twN, float2* twF, int N) {
-    const int e = blockIdx.x * blockDim.x + threadIdx.x;
-    if (e < N) {
-        double s, c;
-        sincospi(-2.0 * (double)e / (double)N, &s, &c);
-        twN[e] = make_float2((float)c, (float)s);
-        sincospi(-(double)e / (double)N, &s, &c);
-        twF[e] = make_float2((float)c, (float)s);
-    }
-}
-
 template <int N>
 static void noalloc_n(const NoallocDevice& d, const float* x, const float* C, int64_t n, int m, int k, int F,
                       int clamp2, int32_t* labels, float* dist, cudaStream_t s) {
     float2* twN = d.scratch;
     float2* twF = twN + N;
     float2* spec = twF + N;
-    k_noalloc_twiddles<<<ceil_div(N, 256), 256, 0, s>>>(twN, twF, N);
+    k_twiddles<<<ceil_div(N, 256), 256, 0, s>>>(twN, twF, N);
     TC_CHECK_LAUNCH();
     const size_t ssm = Cfg<N>::BUF_BYTES + sizeof(TeamScratch);
     allow_max_dynamic_smem(k_centroid_spectra<N>);

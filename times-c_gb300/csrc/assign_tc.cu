@@ -459,13 +459,33 @@ bool screen_supported(int m, int F, int k) {
 // Bound on |d_BF16 - d_FP32| for one (series, centroid) pair.  With x~ = x(1+e1),
 // c~ = c(1+e2), |e| <= 2^-9 (BF16 rounding), every lag's |x~.c~ - x.c| <= (2^-8 + 2^-18)
 // sum |x_i c_j| <= (2^-8 + 2^-18) |x||c| (Cauchy-Schwarz); the norms are FP32 in both
-// kernels.  Allowances: tensor-core FP32 accumulation over mp terms (mp * 2^-21, with
-// room for truncating adders) and the FP32 FFT kernel's own error (1e-5).  A max over
-// lags and the clamp at 2 do not widen it.  If d32(j*) is the FP32 minimum and d16(jb)
-// the BF16 one, d16(j*) <= d32(j*) + D <= d32(jb) + D <= d16(jb) + 2D: every centroid
-// that can be the FP32 first minimum (ties included) has d16 <= min d16 + 2D.
-static float screen_threshold(int mp) {
-    const double D = std::ldexp(1.0, -8) + std::ldexp(1.0, -18) + mp * std::ldexp(1.0, -21) + 1e-5;
+// kernels.  Allowances: the tensor cores' FP32 accumulation over mp terms (mp * 2^-21,
+// with room for truncating adders) and the FP32 FFT kernel's own error (fft_error).  A
+// max over lags and the clamp at 2 do not widen it.  If d32(j*) is the FP32 minimum and
+// d16(jb) the BF16 one, d16(j*) <= d32(j*) + D <= d32(jb) + D <= d16(jb) + 2D: every
+// centroid that can be the FP32 first minimum (ties included) has d16 <= min d16 + 2D.
+//
+// fft_error: a worst-case bound on one lag of the FP32 FFT correlation of unit-norm x
+// and c.  Per transform of length F, the computed spectrum satisfies
+// |y^ - y|_2 <= L eta |y|_2 (1 + O(L eta)), L = log2 F, eta = mu + gamma_4 (sqrt 2 + mu),
+// gamma_4 = 4u/(1 - 4u), u = 2^-24, mu the twiddles' error (<= 2^-24: FP64 sincospi
+// rounded to float) - the radix-2 result of Higham, Accuracy and Stability of Numerical
+// Algorithms (2nd ed.), Thm 24.2, taken per level (a radix-4 or radix-8 pass counts as
+// two or three levels).  |X|_2 = sqrt(F) for the series, |C|_inf <= |c|_1 <= sqrt(m) for
+// the centroid, so the errors of the two forward transforms and of the product
+// (sqrt 2 gamma_2 per bin) reach the correlation as at most (2 L eta + 3u) sqrt(m) in
+// 2-norm after the 1/F-scaled inverse, whose own error adds L eta |r|_2 <= L eta sqrt(m)
+// (|r|_2 <= |x|_1 |c|_2 <= sqrt(m), Young).  A lag's error is at most the 2-norm; the
+// bound is doubled for the normalisation's few roundings and the O(L eta) terms.
+static double fft_error(int m, int F) {
+    const double u = std::ldexp(1.0, -24), g4 = 4 * u / (1 - 4 * u);
+    const double eta = u + g4 * (std::sqrt(2.0) + u);
+    const double L = std::log2((double)F);
+    return 2.0 * (3.0 * L * eta + 3.0 * u) * std::sqrt((double)m);
+}
+
+static float screen_threshold(int mp, int m, int F) {
+    const double D = std::ldexp(1.0, -8) + std::ldexp(1.0, -18) + mp * std::ldexp(1.0, -21) + fft_error(m, F);
     return (float)(2.0 * D * (1.0 + 1e-3));
 }
 
@@ -506,7 +526,7 @@ void launch_assign_tc(tc_ctx* ctx, const AssignArgs& a, int precision, cudaStrea
     if (a.cand) {
         p.cand = a.cand;
         p.ncand = a.ncand;
-        p.thr = screen_threshold(g.mp);
+        p.thr = screen_threshold(g.mp, a.m, a.F);
         p.labels = nullptr;
         p.dist = nullptr;
         p.old_labels = nullptr;

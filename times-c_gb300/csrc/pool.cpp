@@ -13,8 +13,11 @@
 // to its footprint, so while it runs that much is reserved on top of what the
 // worker held; when it ends the reservation is replaced by the bytes actually
 // held.  A worker may take the oldest queued job with held + reserved +
-// footprint <= budget.  If nothing fits, idle workers hand their workspaces back
-// first; a job larger than the whole budget is rejected at submission.
+// footprint <= budget; a job that has waited at the head of the queue for more
+// than TIMESC_POOL_HEAD_WAIT_S seconds (default 2) is the only one that may
+// start, so small jobs cannot overtake a large one forever.  Idle workers hand
+// their workspaces back when that lets a job start (pool_sched.h); a job larger
+// than the whole budget is rejected at submission.
 #include <algorithm>
 #include <chrono>
 #include <cstdio>
@@ -26,6 +29,7 @@
 #include <unordered_map>
 #include <vector>
 
+#include "pool_sched.h"
 #include "tc_internal.h"
 
 namespace {
@@ -67,6 +71,7 @@ struct tc_pool {
     uint64_t next_ticket = 1;
     int running = 0;
     bool stopping = false;
+    double head_wait_s = 2.0;     // after this long at the head of the queue a job has priority
 
     uint64_t held_total() const {
         uint64_t t = 0;
@@ -74,31 +79,39 @@ struct tc_pool {
         return t;
     }
 
-    // Under mu: the first queued ticket worker w may start (its footprint is then
-    // reserved), releasing idle workspaces if that makes one fit.  0 if none.
+    // Under mu: the queued ticket worker w may start (its footprint is then
+    // reserved), releasing idle workspaces where that lets a job start (the rules
+    // of sched_pick).  0 if none.
     uint64_t pick(int w) {
         for (int pass = 0; pass < 2; ++pass) {
-            for (auto it = queue.begin(); it != queue.end(); ++it) {
-                const Request& r = reqs[*it];
-                if (held_total() + r.footprint <= budget) {
-                    const uint64_t t = *it;
-                    resv[w] = r.footprint;
-                    queue.erase(it);
-                    return t;
+            std::vector<tc::SchedJob> q;
+            q.reserve(queue.size());
+            const Clock::time_point now = Clock::now();
+            for (uint64_t t : queue) {
+                const Request& r = reqs[t];
+                q.push_back(tc::SchedJob{r.footprint, std::chrono::duration<double>(now - r.submitted).count()});
+            }
+            tc::SchedWorkers ws;
+            ws.budget = budget;
+            ws.held = held;
+            ws.resv = resv;
+            ws.busy = busy;
+            const tc::SchedChoice c = tc::sched_pick(q, ws, head_wait_s);
+            if (c.index >= 0) {
+                auto it = queue.begin() + c.index;
+                const uint64_t t = *it;
+                resv[w] = reqs[t].footprint;
+                queue.erase(it);
+                return t;
+            }
+            if (!c.release_idle || pass == 1) break;
+            for (size_t v = 0; v < ctx.size(); ++v)  // idle workers (this one included) hand back their buffers
+                if (!busy[v] && held[v] > 0) {
+                    cudaSetDevice(device);
+                    cudaStreamSynchronize(ctx[v]->own_stream);
+                    tc::release_workspace(ctx[v]);
+                    held[v] = 0;
                 }
-            }
-            if (pass == 0) {  // make room: idle workers (this one included) hand back their buffers
-                bool freed = false;
-                for (size_t v = 0; v < ctx.size(); ++v)
-                    if (!busy[v] && held[v] > 0) {
-                        cudaSetDevice(device);
-                        cudaStreamSynchronize(ctx[v]->own_stream);
-                        tc::release_workspace(ctx[v]);
-                        held[v] = 0;
-                        freed = true;
-                    }
-                if (!freed) break;
-            }
         }
         return 0;
     }
@@ -207,6 +220,7 @@ int tc_pool_create(int device, const tc_pool_opts* opts, tc_pool** out) {
     tc_pool* p = new (std::nothrow) tc_pool();
     if (!p) return TC_ERR_NOMEM;
     p->device = device;
+    if (const char* hw = std::getenv("TIMESC_POOL_HEAD_WAIT_S")) p->head_wait_s = std::atof(hw);
     if (opts && opts->hbm_budget_bytes > 0) {
         p->budget = opts->hbm_budget_bytes;
     } else {

@@ -11,6 +11,7 @@
 #include <vector>
 
 #include "timesc.h"
+#include "screen.cuh"
 
 // ---------------------------------------------------------------- errors
 struct TcError {
@@ -192,7 +193,6 @@ struct AssignArgs {
     int32_t* cand;
     int32_t* ncand;
 };
-constexpr int SCREEN_CAP = 8;
 void launch_assign_fft(tc_ctx* ctx, const AssignArgs& a, cudaStream_t s);
 
 // tensor-core correlation (tcgen05); returns false when the shape is not supported
