@@ -223,21 +223,12 @@ def cpu_iteration(O, X, C, labels, mode, F, ns):
     return time.perf_counter() - t0
 
 
-def cpu_sample_iteration(O, X, C, labels, mode, F, target_s, n_full):
-    """Oracle iterations (extract + assign) on two sample sizes; the iteration
-    time at n_full series is extrapolated linearly (the eigenvector step costs
-    the same at any n, the rest grows with n)."""
-    n = X.shape[0]
-    ns = min(n, 1024)
-    while True:
-        dt = cpu_iteration(O, X, C, labels, mode, F, ns)
-        if dt >= 0.5 * target_s or ns >= n:
-            break
-        ns = min(n, int(ns * max(2.0, 0.7 * target_s / max(dt, 1e-3))))
-    dt_half = cpu_iteration(O, X, C, labels, mode, F, ns // 2)
-    slope = max(dt - dt_half, 1e-9) / (ns - ns // 2)
-    fixed = max(dt - slope * ns, 0.0)
-    return ns, dt, fixed + slope * n_full
+def arm_config(args, wl, F, world):
+    """The `config` both arms print (the driver compares them)."""
+    n, m, k, noise, dirich, desc = wl
+    return {"workload": desc, "mode": args.mode, "precision": args.precision, "fft_length": F,
+            "parallelism": "replicas" if world > 1 else "single GPU",
+            "l2": "inputs larger than L2 (%.1f GB of series)" % (4 * n * m / 1e9)}
 
 
 def host_threads():
@@ -260,42 +251,45 @@ def max_over_ranks(value, dist):
 
 
 def run_reference(args, wl):
-    """The reference's CPU implementation of the path (FP64 port), rank 0 only."""
+    """The reference's CPU implementation of the path, rank 0 only.  Its own CPU code
+    (Code/test/test_timesC.py) does not reach GPU hosts (and at this size would need
+    ~0.5 TB per temporary), so the FP64 port of the reference's GPU path (oracle/)
+    runs on all host threads.  The series come from the oracle library's copy of
+    the generator: nothing of the engine is loaded.  Warm-up steps run on a tenth
+    of the series; every timed step is one whole iteration (extraction + SBD
+    assignment) over all n series."""
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return
-    import timesc
+    os.environ.setdefault("OMP_NUM_THREADS", str(host_threads()))
     from oracle import oracle as O
     n, m, k, noise, dirich, desc = wl
-    os.environ.setdefault("OMP_NUM_THREADS", str(host_threads()))
-    data, truth = timesc.generate(n, m, k, noise=noise, dirichlet=dirich, seed=0)
-    X = O.znorm(data[: min(n, 200_000)].astype(np.float64))
+    data, _ = O.generate(n, m, k, noise=noise, dirichlet=dirich, seed=0)
+    X = O.znorm(data.astype(np.float64))
+    del data
     rng = np.random.default_rng(0)
-    labels = rng.integers(0, k, size=X.shape[0]).astype(np.int32)
-    C = X[rng.choice(X.shape[0], k, replace=False)].copy()
+    labels = rng.integers(0, k, size=n).astype(np.int32)
+    C = X[rng.choice(n, k, replace=False)].copy()
     C /= np.linalg.norm(C, axis=1, keepdims=True)
     md = MODES[args.mode]
     F = O.fft_size(m, md)
-    ns, _, _ = cpu_sample_iteration(O, X, C, labels, md, F, target_s=3.0, n_full=n)
-    half = cpu_iteration(O, X, C, labels, md, F, ns // 2)
-    full_est = []
-    for s in range(args.warmup + args.steps):
-        dt = cpu_iteration(O, X, C, labels, md, F, ns)
-        slope = max(dt - half, 1e-9) / (ns - ns // 2)
-        if s >= args.warmup:
-            full_est.append(max(dt - slope * ns, 0.0) + slope * n)
-    t = statistics.mean(full_est)
+    nw = max(k, n // 10)
+    for _ in range(args.warmup):
+        cpu_iteration(O, X, C, labels, md, F, nw)
+    times = [cpu_iteration(O, X, C, labels, md, F, n) for _ in range(args.steps)]
+    t = statistics.mean(times)
     value = n * k / t
     line = {"impl": "reference", "metric": "SBD pairs/s (whole k-Shape iterations)", "value": value,
             "unit": "pairs/s", "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": 1e3 * t, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": desc, "mode": args.mode, "sample_series": ns},
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic (prototype generator)",
+            "config": arm_config(args, wl, F, int(os.environ.get("WORLD_SIZE", "1"))),
             "cpu_baseline": {"value": value, "unit": "pairs/s", "cores": int(os.environ["OMP_NUM_THREADS"]),
                              "kind": "port",
-                             "sample": "per step one extract+assign of the FP64 oracle on %d of %d series (all %d "
-                                       "centroids); full-n time extrapolated from %d and %d series"
-                                       % (ns, n, k, ns, ns // 2)},
+                             "sample": "every timed step one whole extract + assign iteration of the FP64 port "
+                                       "over all %d series and %d centroids (no extrapolation); warm-up steps "
+                                       "over %d series" % (n, k, nw),
+                             "step_s": times},
             "e2e": {"value": value, "unit": "pairs/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line))
 
@@ -353,38 +347,103 @@ def plain_fp32_compare(ctx, x, labels, C, n, m, k, mode, prec, stream, ms_mixed,
            "label_agreement": float((L32 == L16).mean()), "ari": ari(L32, L16),
            "what": "mixed vs plain FP32 over all n: extraction from the same labels, assignment against "
                    "the same FP32 centroids (the FP32 form is parity-tested against the FP64 oracle)"}
-    # timing: whole iterations and the assignment in FP32
-    e0, e1, a0, a1 = (torch.cuda.Event(enable_timing=True) for _ in range(4))
-    lab = lab0.clone()
-    old = lab0.clone()
-    ch = torch.zeros(1, dtype=torch.int32, device="cuda")
-    ds = torch.zeros(1, dtype=torch.float64, device="cuda")
-    dist = torch.empty_like(d32)
-    for _ in range(2):  # warm
-        ctx.extract_shapes(x, lab, C32, mode=mode, precision=PREC["fp32"])
-        ctx.sbd_assign(x, C32, mode=mode, precision=PREC["fp32"], labels=lab, dist=dist)
-    torch.cuda.synchronize()
-    a_tot = 0.0
-    e0.record(stream)
-    for _ in range(steps):
-        ctx.extract_shapes(x, lab, C32, mode=mode, precision=PREC["fp32"])
-        ch.zero_()
-        ds.zero_()
-        a0.record(stream)
-        ctx.sbd_assign(x, C32, mode=mode, precision=PREC["fp32"], labels=lab, dist=dist, old_labels=old,
-                       changed=ch, dist_sum=ds)
-        a1.record(stream)
-        ch.item()
-        a_tot += a0.elapsed_time(a1)
-    e1.record(stream)
-    torch.cuda.synchronize()
-    ms32 = e0.elapsed_time(e1) / steps
-    a32 = a_tot / steps
+    # timing: whole iterations and the assignment in FP32, screened (the product's FP32
+    # form) and unscreened (every centroid through the FFT kernel: the plain FP32 form)
+    def time_fp32():
+        e0, e1, a0, a1 = (torch.cuda.Event(enable_timing=True) for _ in range(4))
+        lab = lab0.clone()
+        old = lab0.clone()
+        Cw = C32.clone()
+        ch = torch.zeros(1, dtype=torch.int32, device="cuda")
+        ds = torch.zeros(1, dtype=torch.float64, device="cuda")
+        dist = torch.empty_like(d32)
+        for _ in range(2):  # warm
+            ctx.extract_shapes(x, lab, Cw, mode=mode, precision=PREC["fp32"])
+            ctx.sbd_assign(x, Cw, mode=mode, precision=PREC["fp32"], labels=lab, dist=dist)
+        torch.cuda.synchronize()
+        a_tot = 0.0
+        e0.record(stream)
+        for _ in range(steps):
+            ctx.extract_shapes(x, lab, Cw, mode=mode, precision=PREC["fp32"])
+            ch.zero_()
+            ds.zero_()
+            a0.record(stream)
+            ctx.sbd_assign(x, Cw, mode=mode, precision=PREC["fp32"], labels=lab, dist=dist, old_labels=old,
+                           changed=ch, dist_sum=ds)
+            a1.record(stream)
+            ch.item()
+            a_tot += a0.elapsed_time(a1)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / steps, a_tot / steps
+
+    ms32, a32 = time_fp32()
+    os.environ["TIMESC_NO_SCREEN"] = "1"
+    try:
+        ms_u, a_u = time_fp32()
+    finally:
+        del os.environ["TIMESC_NO_SCREEN"]
     rep.update({"ms_per_iteration": ms32, "assign_ms": a32, "assign_pairs_per_s": n * k / (a32 / 1e3),
                 "pairs_per_s_whole_iterations": n * k / (ms32 / 1e3),
                 "mixed_vs_plain_fp32_assign_speedup": a32 / a_ms_mixed,
-                "mixed_vs_plain_fp32_iteration_speedup": ms32 / ms_mixed})
+                "mixed_vs_plain_fp32_iteration_speedup": ms32 / ms_mixed,
+                "unscreened": {"ms_per_iteration": ms_u, "assign_ms": a_u,
+                               "pairs_per_s_whole_iterations": n * k / (ms_u / 1e3),
+                               "assign_pairs_per_s": n * k / (a_u / 1e3),
+                               "mixed_speedup_iteration": ms_u / ms_mixed,
+                               "mixed_speedup_assign": a_u / a_ms_mixed,
+                               "what": "the plain FP32 form: every centroid through the FP32 FFT kernel "
+                                       "(TIMESC_NO_SCREEN=1), the denominator of the mixed form's speed-up"}})
     return rep
+
+
+def oracle_iteration_report(ctx, data, x, labels, C, n, m, k, mode, F, prec):
+    """One whole iteration of the FP64 oracle over all n series from the timed run's
+    final state (labels, centroids): its time is the CPU baseline (all host threads,
+    no extrapolation), its outputs the reference for the GPU forms' errors.  Each
+    GPU form runs the same iteration from the same state: its centroid error, its
+    SBD error (assignment against the oracle's centroids, so that only the
+    assignment's arithmetic differs) and the ARI of its own iteration's labels."""
+    import torch
+    from oracle import oracle as O
+    X = O.znorm(data.astype(np.float64))
+    lab_h = labels.cpu().numpy().astype(np.int32)
+    C_h = C.cpu().numpy().astype(np.float64)
+    om = O.MODE_COMPAT if mode == 0 else O.MODE_CANONICAL
+    clamp2 = mode == 0 and 2 * m - 1 < 512
+    t0 = time.perf_counter()
+    C_o, _, _ = O.extract(X, lab_h, C_h, om)
+    l_o, d_o, _, margin = O.assign(X, C_o, F, clamp2=clamp2)
+    t = time.perf_counter() - t0
+    del X
+    base = {"value": n * k / t, "unit": "pairs/s", "cores": host_threads(), "kind": "port",
+            "sample": "one whole extract + assign iteration of the FP64 oracle over all %d series and %d centroids "
+                      "(%.1f s, no extrapolation), from the timed run's final state" % (n, k, t)}
+    rep = {"what": "one iteration (extraction from the timed run's final labels and centroids, then assignment) "
+                   "of each GPU form against the FP64 oracle over all %d series" % n,
+           "oracle_min_margin": float(margin.min()) if k > 1 else None}
+    c_o = torch.from_numpy(C_o.astype(np.float32)).cuda()
+    forms = [("fp32", PREC["fp32"])] + ([(args_prec_name(prec), prec)] if prec != PREC["fp32"] else [])
+    for name, p in forms:
+        Cg = C.clone()
+        ctx.extract_shapes(x, labels.clone(), Cg, mode=mode, precision=p)
+        lg = torch.empty_like(labels)
+        dg = torch.empty((n,), dtype=torch.float32, device="cuda")
+        ctx.sbd_assign(x, Cg, mode=mode, precision=p, labels=lg, dist=dg)
+        ls = torch.empty_like(labels)
+        ds = torch.empty_like(dg)
+        ctx.sbd_assign(x, c_o, mode=mode, precision=p, labels=ls, dist=ds)
+        torch.cuda.synchronize()
+        L = lg.cpu().numpy()
+        rep[name] = {"centroid_max_abs_err": float(np.abs(Cg.cpu().numpy() - C_o).max()),
+                     "sbd_max_abs_err": float(np.abs(ds.cpu().numpy() - d_o).max()),
+                     "ari": ari(L, l_o), "label_agreement": float((L == l_o).mean()),
+                     "labels_vs_oracle_on_oracle_centroids": float((ls.cpu().numpy() == l_o).mean())}
+    return base, rep
+
+
+def args_prec_name(prec):
+    return {v: k for k, v in PREC.items()}[prec]
 
 
 # ---------------------------------------------------------------- many jobs (batch, serving)
@@ -698,9 +757,7 @@ def main():
                "dtype": ("bf16 operands, f32 accumulation" if tc_supported(m, F, prec) else
                          "f32 (exact BF16 screening pass)" if screened(m, F, k, prec) else "f32"),
                "data": "synthetic (prototype generator: sinusoids + bump, shifted/scaled/offset, noise)",
-               "config": {"workload": desc, "mode": args.mode, "precision": args.precision, "fft_length": F,
-                          "parallelism": "replicas" if world > 1 else "single GPU",
-                          "l2": "inputs larger than L2 (%.1f GB of series)" % (4 * n * m / 1e9)},
+               "config": arm_config(args, wl, F, world),
                "kshape_iters_per_s": 1e3 / ms_step,
                "assign_pairs_per_s": n * k / (a_ms / 1e3),
                "roofline": roof, "gpu_launches": int(launches), "clocks": clocks}
@@ -719,30 +776,35 @@ def main():
                                    "what": "materialising NCC_3D + get_pos_idx on cuFFT (torch.fft), FP32, chunked"}
         out["fused_vs_cufft_assign_speedup"] = cu_ms / a_ms
 
-    # end-to-end through the public C ABI with pinned host buffers
+    # end-to-end through the public C ABI with pinned host buffers: every step is one
+    # call that copies the series in, z-normalises them, runs one whole iteration and
+    # copies labels and centroids out
     if not args.no_e2e:
         pinned = torch.empty((n, m), dtype=torch.float32, pin_memory=True)
         pinned.numpy()[:] = data
-        e_iters = 3
-        ctx.kshape_run(pinned.numpy(), k, mode=mode, precision=prec, max_iter=1, restart=False)  # warm
+        for _ in range(2):  # warm: the first call issues its stages directly, the second captures their graphs
+            ctx.kshape_run(pinned.numpy(), k, mode=mode, precision=prec, max_iter=1, restart=False)
+        walls = []
+        for _ in range(3):
+            t0 = time.perf_counter()
+            r = ctx.kshape_run(pinned.numpy(), k, mode=mode, precision=prec, max_iter=1, restart=False)
+            walls.append(time.perf_counter() - t0)
+        wall = statistics.mean(walls)
         t0 = time.perf_counter()
-        r = ctx.kshape_run(pinned.numpy(), k, mode=mode, precision=prec, max_iter=e_iters, restart=False)
-        wall = time.perf_counter() - t0
+        r3 = ctx.kshape_run(pinned.numpy(), k, mode=mode, precision=prec, max_iter=3, restart=False)
+        wall3 = time.perf_counter() - t0
+        e2e_val = max_over_ranks(wall, dist)  # every rank takes part
         if out is not None:
-            out["e2e"] = {"value": world * n * k * r["iterations"] / wall, "unit": "pairs/s",
+            out["e2e"] = {"value": world * n * k * r["iterations"] / e2e_val, "unit": "pairs/s",
                           "h2d_bytes_per_step": 4 * n * m, "d2h_bytes_per_step": 4 * n + 4 * k * m,
-                          "iterations": r["iterations"], "wall_s": wall,
-                          "call": "tc_kshape_run(h_data pinned, max_iter=%d, restart=0)" % e_iters}
+                          "step": "one tc_kshape_run call (h_data pinned, max_iter=1, restart=0): series in, "
+                                  "z-norm, one whole iteration, labels and centroids out",
+                          "wall_s_per_call": walls,
+                          "three_iteration_call": {"iterations": r3["iterations"], "wall_s": wall3,
+                                                   "pairs_per_s": n * k * r3["iterations"] / wall3}}
     if out is not None and not args.no_cpu:
-        from oracle import oracle as O
-        X = O.znorm(data[:100_000].astype(np.float64))
-        lab_h = labels[:100_000].cpu().numpy()
-        C_h = C.cpu().numpy().astype(np.float64)
-        ns, dt, t_full = cpu_sample_iteration(O, X, C_h, lab_h, mode, F, target_s=10.0, n_full=n)
-        out["cpu_baseline"] = {"value": n * k / t_full, "unit": "pairs/s", "cores": host_threads(), "kind": "port",
-                               "sample": "one extract+assign iteration of the FP64 oracle on %d and %d of the %d "
-                                         "series (all %d centroids), extrapolated to all series; %.1f s measured"
-                                         % (ns, ns // 2, n, k, dt)}
+        out["cpu_baseline"], out["fp64_oracle_report"] = oracle_iteration_report(ctx, data, x, labels, C, n, m, k,
+                                                                                 mode, F, prec)
     if out is not None:
         print(json.dumps(out))
     ctx.close()

@@ -6,6 +6,8 @@
 // relative to the Times-C project root).
 #include "oracle.h"
 
+#include "gen_core.h"  // the synthetic workloads (header-only; the engine library is not linked)
+
 #include <algorithm>
 #include <cmath>
 #include <complex>
@@ -26,6 +28,7 @@ namespace {
 struct FftPlan {
     int n = 0;
     std::vector<cd> roots;      // exp(-2 pi i j / n)
+    std::vector<cd> iroots;     // their conjugates (inverse transform)
     std::vector<int> rev;
     void init(int n_) {
         n = n_;
@@ -34,6 +37,8 @@ struct FftPlan {
             double a = -2.0 * M_PI * (double)j / (double)n;
             roots[j] = cd(std::cos(a), std::sin(a));
         }
+        iroots.resize(n);
+        for (int j = 0; j < n; ++j) iroots[j] = std::conj(roots[j]);
         rev.assign(n, 0);
         int lg = 0;
         while ((1 << lg) < n) ++lg;
@@ -48,12 +53,12 @@ struct FftPlan {
     void run(cd* a, bool inverse) const {
         for (int i = 0; i < n; ++i)
             if (i < rev[i]) std::swap(a[i], a[rev[i]]);
+        const cd* rt = inverse ? iroots.data() : roots.data();
         for (int len = 2; len <= n; len <<= 1) {
             int half = len >> 1, step = n / len;
             for (int i = 0; i < n; i += len)
                 for (int j = 0; j < half; ++j) {
-                    cd w = roots[j * step];
-                    if (inverse) w = std::conj(w);
+                    const cd w = rt[j * step];
                     cd u = a[i + j], v = a[i + j + half] * w;
                     a[i + j] = u + v;
                     a[i + j + half] = u - v;
@@ -75,6 +80,26 @@ void circ_corr_spec(const std::vector<cd>& X, const std::vector<cd>& Y, const Ff
     for (int f = 0; f < F; ++f) work[f] = X[f] * std::conj(Y[f]);
     p.run(work.data(), true);
     for (int f = 0; f < F; ++f) r[f] = work[f].real() / F;
+}
+
+// The same correlation through a complex transform of half the length (Z = X conj(Y)
+// is Hermitian, so r is real): with N = F/2, A[k] = Z[k] + Z[k+N] and
+// B[k] = (Z[k] - Z[k+N]) exp(2 pi i k/F), the inverse transform of A + iB holds
+// r[2t] in its real and r[2t+1] in its imaginary parts.  pF: length F, pN: F/2.
+void circ_corr_half(const std::vector<cd>& X, const std::vector<cd>& Y, const FftPlan& pF, const FftPlan& pN,
+                    std::vector<cd>& work, double* r) {
+    const int F = pF.n, N = F / 2;
+    for (int f = 0; f <= N; ++f) work[f] = X[f] * std::conj(Y[f]);  // Z[0..N]
+    cd* c = work.data() + N + 1;                                    // N values after Z[0..N]
+    for (int q = 0; q < N; ++q) {
+        const cd z0 = work[q], z1 = std::conj(work[N - q]);  // Z[q], Z[q+N]
+        c[q] = (z0 + z1) + cd(0, 1) * ((z0 - z1) * pF.iroots[q]);
+    }
+    pN.run(c, true);
+    for (int t = 0; t < N; ++t) {
+        r[2 * t] = c[t].real() / F;
+        r[2 * t + 1] = c[t].imag() / F;
+    }
 }
 
 void spectrum(const double* x, int m, const FftPlan& p, std::vector<cd>& out) {
@@ -165,8 +190,9 @@ void or_ncc_naive(const double* x, const double* y, int m, int F, double* out) {
 // (first centroid wins ties, :82-86).
 void or_assign(const double* X, const double* C, int64_t n, int m, int k, int F, int clamp2,
                int32_t* labels, double* dist, int32_t* shift, double* margin) {
-    FftPlan p;
+    FftPlan p, ph;
     p.init(F);
+    ph.init(F / 2);
     std::vector<std::vector<cd>> Cs(k);
     std::vector<double> cn(k);
     for (int j = 0; j < k; ++j) {
@@ -175,9 +201,11 @@ void or_assign(const double* X, const double* C, int64_t n, int m, int k, int F,
     }
     const int L = 2 * m - 1;
     const bool pad2 = clamp2 && L < 512;
+    std::vector<int> slot(L);
+    for (int s = 0; s < L; ++s) slot[s] = slot_to_circ(s, m, F);
 #pragma omp parallel
     {
-        std::vector<cd> Xs, work(F);
+        std::vector<cd> Xs, work(F + 2);
         std::vector<double> r(F);
 #pragma omp for schedule(dynamic, 16)
         for (int64_t i = 0; i < n; ++i) {
@@ -187,13 +215,13 @@ void or_assign(const double* X, const double* C, int64_t n, int m, int k, int F,
             double best = 1e300, second = 1e300;
             int bj = 0, bshift = 0;
             for (int j = 0; j < k; ++j) {
-                circ_corr_spec(Xs, Cs[j], p, work, r.data());
+                circ_corr_half(Xs, Cs[j], p, ph, work, r.data());
                 double den = xn * cn[j];
                 double dmin = 1e300;
                 int last_arg = 0;
                 double vmax = -1e300;
                 for (int s = 0; s < L; ++s) {
-                    double v = den == 0 ? 0.0 : r[slot_to_circ(s, m, F)] / den;
+                    double v = den == 0 ? 0.0 : r[slot[s]] / den;
                     double d = 1.0 - v;
                     if (d < dmin) dmin = d;
                     if (v >= vmax) { vmax = v; last_arg = s; }
@@ -218,48 +246,144 @@ void or_assign(const double* X, const double* C, int64_t n, int m, int k, int F,
 }
 
 // cyclic Jacobi eigen-solver (stands in for cusolverDnSsyevd, shapeExtract.cuh:434-445).
+// Top eigenpair of a symmetric matrix (stands in for the last column of
+// cusolverDnSsyevd, shapeExtract.cuh:434-445 and :658-689): Householder
+// reduction to tridiagonal form (Golub & Van Loan, Matrix Computations, Alg.
+// 8.3.1), the largest eigenvalue of the tridiagonal matrix by Sturm-sequence
+// bisection, its eigenvector by inverse iteration (tridiagonal elimination with
+// partial pivoting), transformed back by the Householder reflectors.  A zero
+// matrix gives the last basis vector, the last column of the identity
+// eigenbasis a symmetric eigensolver returns for it.
 double or_top_eig_jacobi(const double* Ain, int m, double* vec) {
-    std::vector<double> A(Ain, Ain + (size_t)m * m), V((size_t)m * m, 0.0);
-    for (int i = 0; i < m; ++i) V[(size_t)i * m + i] = 1.0;
-    for (int sweep = 0; sweep < 100; ++sweep) {
-        double off = 0, tot = 0;
-        for (int i = 0; i < m; ++i)
-            for (int j = 0; j < m; ++j) {
-                double a = A[(size_t)i * m + j];
-                tot += a * a;
-                if (i != j) off += a * a;
-            }
-        if (off <= 1e-30 * (tot + 1e-300)) break;
-        for (int p = 0; p < m - 1; ++p)
-            for (int q = p + 1; q < m; ++q) {
-                double apq = A[(size_t)p * m + q];
-                if (std::fabs(apq) < 1e-300) continue;
-                double app = A[(size_t)p * m + p], aqq = A[(size_t)q * m + q];
-                double theta = (aqq - app) / (2 * apq);
-                double t = (theta >= 0 ? 1.0 : -1.0) / (std::fabs(theta) + std::sqrt(theta * theta + 1));
-                double c = 1 / std::sqrt(t * t + 1), s = t * c;
-                for (int r = 0; r < m; ++r) {  // A = A * J
-                    double arp = A[(size_t)r * m + p], arq = A[(size_t)r * m + q];
-                    A[(size_t)r * m + p] = c * arp - s * arq;
-                    A[(size_t)r * m + q] = s * arp + c * arq;
-                }
-                for (int r = 0; r < m; ++r) {  // A = J^T * A
-                    double apr = A[(size_t)p * m + r], aqr = A[(size_t)q * m + r];
-                    A[(size_t)p * m + r] = c * apr - s * aqr;
-                    A[(size_t)q * m + r] = s * apr + c * aqr;
-                }
-                for (int r = 0; r < m; ++r) {
-                    double vrp = V[(size_t)r * m + p], vrq = V[(size_t)r * m + q];
-                    V[(size_t)r * m + p] = c * vrp - s * vrq;
-                    V[(size_t)r * m + q] = s * vrp + c * vrq;
-                }
-            }
+    std::vector<double> A(Ain, Ain + (size_t)m * m);
+    double fro = 0;
+    for (double a : A) fro += a * a;
+    if (!(fro > 0)) {
+        for (int r = 0; r < m; ++r) vec[r] = r == m - 1 ? 1.0 : 0.0;
+        return 0.0;
     }
-    int best = 0;
-    for (int i = 1; i < m; ++i)
-        if (A[(size_t)i * m + i] >= A[(size_t)best * m + best]) best = i;
-    for (int r = 0; r < m; ++r) vec[r] = V[(size_t)r * m + best];
-    return A[(size_t)best * m + best];
+    // reflectors H_k = I - 2 v_k v_k^T on indices k+1..m-1, stored in V (row k)
+    std::vector<double> V((size_t)m * m, 0.0), p(m), w(m);
+    for (int k = 0; k + 2 < m; ++k) {
+        const int n = m - k - 1;
+        double xn = 0;
+        for (int i = 0; i < n; ++i) xn += A[(size_t)(k + 1 + i) * m + k] * A[(size_t)(k + 1 + i) * m + k];
+        xn = std::sqrt(xn);
+        if (xn == 0) continue;
+        const double x0 = A[(size_t)(k + 1) * m + k];
+        const double alpha = x0 > 0 ? -xn : xn;
+        double* v = &V[(size_t)k * m];
+        for (int i = 0; i < n; ++i) v[i] = A[(size_t)(k + 1 + i) * m + k];
+        v[0] -= alpha;
+        double vn = 0;
+        for (int i = 0; i < n; ++i) vn += v[i] * v[i];
+        vn = std::sqrt(vn);
+        if (vn == 0) continue;
+        for (int i = 0; i < n; ++i) v[i] /= vn;
+        // B = A[k+1:, k+1:]:  p = 2 B v, q = p - (v.p) v, B -= v q^T + q v^T
+        for (int i = 0; i < n; ++i) {
+            const double* Bi = &A[(size_t)(k + 1 + i) * m + k + 1];
+            double s2 = 0;
+            for (int j = 0; j < n; ++j) s2 += Bi[j] * v[j];
+            p[i] = 2 * s2;
+        }
+        double K = 0;
+        for (int i = 0; i < n; ++i) K += v[i] * p[i];
+        for (int i = 0; i < n; ++i) w[i] = p[i] - K * v[i];
+        for (int i = 0; i < n; ++i) {
+            double* Bi = &A[(size_t)(k + 1 + i) * m + k + 1];
+            for (int j = 0; j < n; ++j) Bi[j] -= v[i] * w[j] + w[i] * v[j];
+        }
+        A[(size_t)(k + 1) * m + k] = alpha;
+        A[(size_t)k * m + k + 1] = alpha;
+        for (int i = 1; i < n; ++i) {
+            A[(size_t)(k + 1 + i) * m + k] = 0;
+            A[(size_t)k * m + k + 1 + i] = 0;
+        }
+    }
+    std::vector<double> d(m), e(m, 0.0);
+    for (int i = 0; i < m; ++i) d[i] = A[(size_t)i * m + i];
+    for (int i = 0; i + 1 < m; ++i) e[i] = A[(size_t)(i + 1) * m + i];
+    // largest eigenvalue: eigenvalues below x = negative pivots of T - x I
+    auto below = [&](double x) {
+        int c = 0;
+        double q = 1;
+        for (int i = 0; i < m; ++i) {
+            q = (d[i] - x) - (i > 0 ? e[i - 1] * e[i - 1] / q : 0.0);
+            if (q == 0) q = -1e-300;
+            if (q < 0) ++c;
+        }
+        return c;
+    };
+    double lo = d[0], hi = d[0];
+    for (int i = 0; i < m; ++i) {
+        const double r = (i > 0 ? std::fabs(e[i - 1]) : 0.0) + (i + 1 < m ? std::fabs(e[i]) : 0.0);
+        lo = std::min(lo, d[i] - r);
+        hi = std::max(hi, d[i] + r);
+    }
+    for (int it = 0; it < 200 && hi - lo > 4e-16 * std::max(std::fabs(lo), std::fabs(hi)); ++it) {
+        const double mid = 0.5 * (lo + hi);
+        if (below(mid) < m) lo = mid;
+        else hi = mid;
+    }
+    const double lam = hi;
+    // inverse iteration: (T - lam I) y = x, Gaussian elimination with row swaps (the
+    // upper factor gains a second superdiagonal)
+    const double tiny = 1e-300 + 2.2e-16 * std::sqrt(fro);
+    std::vector<double> x(m, 1.0), u0(m), u1(m), u2(m), l(m);
+    std::vector<char> swp(m);
+    for (int i = 0; i < m; ++i) {
+        u0[i] = d[i] - lam;
+        u1[i] = i + 1 < m ? e[i] : 0.0;
+        u2[i] = 0.0;
+    }
+    for (int i = 0; i + 1 < m; ++i) {
+        const double sub = e[i];  // row i+1, column i
+        if (std::fabs(sub) > std::fabs(u0[i])) {  // swap rows i and i+1
+            swp[i] = 1;
+            const double r0 = u0[i], r1 = u1[i], r2 = u2[i];
+            u0[i] = sub;
+            u1[i] = d[i + 1] - lam;
+            u2[i] = i + 2 < m ? e[i + 1] : 0.0;
+            l[i] = r0 / u0[i];
+            u0[i + 1] = r1 - l[i] * u1[i];
+            u1[i + 1] = r2 - l[i] * u2[i];
+        } else {
+            swp[i] = 0;
+            if (u0[i] == 0) u0[i] = tiny;
+            l[i] = sub / u0[i];
+            u0[i + 1] = (d[i + 1] - lam) - l[i] * u1[i];
+            u1[i + 1] = (i + 2 < m ? e[i + 1] : 0.0) - l[i] * u2[i];
+        }
+        u2[i + 1] = 0.0;
+    }
+    if (u0[m - 1] == 0) u0[m - 1] = tiny;
+    for (int it = 0; it < 3; ++it) {
+        for (int i = 0; i + 1 < m; ++i) {  // apply the row operations
+            if (swp[i]) std::swap(x[i], x[i + 1]);
+            x[i + 1] -= l[i] * x[i];
+        }
+        for (int i = m - 1; i >= 0; --i) {  // back substitution
+            double sacc = x[i];
+            if (i + 1 < m) sacc -= u1[i] * x[i + 1];
+            if (i + 2 < m) sacc -= u2[i] * x[i + 2];
+            x[i] = sacc / (u0[i] != 0 ? u0[i] : tiny);
+        }
+        double nn = 0;
+        for (double t : x) nn += t * t;
+        nn = std::sqrt(nn);
+        for (double& t : x) t /= nn;
+    }
+    // back to A's basis: vec = H_0 H_1 ... H_{m-3} x
+    for (int k = m - 3; k >= 0; --k) {
+        const int n = m - k - 1;
+        const double* v = &V[(size_t)k * m];
+        double dot = 0;
+        for (int i = 0; i < n; ++i) dot += v[i] * x[k + 1 + i];
+        for (int i = 0; i < n; ++i) x[k + 1 + i] -= 2 * dot * v[i];
+    }
+    for (int r = 0; r < m; ++r) vec[r] = x[r];
+    return lam;
 }
 
 void or_random_select(int64_t n, int k, uint32_t seed, int32_t* out) {
@@ -318,16 +442,25 @@ int first_argmax(const double* a, int len) {
 }
 
 void gram_centered(const std::vector<double>& Y, int cnt, int m, std::vector<double>& M) {
-    // S = Y^T Y (shapeExtract.cuh:532-537); M = Q S Q with Q = I - 11^T/m (:204-214, :551-570)
+    // S = Y^T Y (shapeExtract.cuh:532-537); M = Q S Q with Q = I - 11^T/m (:204-214, :551-570).
+    // Upper triangle, rows of Y in blocks that stay in cache, each S row a contiguous
+    // axpy per member row.
     std::vector<double> S((size_t)m * m, 0.0);
+    const int RB = 128;
+    for (int i0 = 0; i0 < cnt; i0 += RB) {
+        const int i1 = std::min(cnt, i0 + RB);
 #pragma omp parallel for schedule(dynamic, 4)
-    for (int a = 0; a < m; ++a)
-        for (int b = a; b < m; ++b) {
-            double s = 0;
-            for (int i = 0; i < cnt; ++i) s += Y[(size_t)i * m + a] * Y[(size_t)i * m + b];
-            S[(size_t)a * m + b] = s;
-            S[(size_t)b * m + a] = s;
+        for (int a = 0; a < m; ++a) {
+            double* Sa = &S[(size_t)a * m];
+            for (int i = i0; i < i1; ++i) {
+                const double* y = &Y[(size_t)i * m];
+                const double ya = y[a];
+                for (int b = a; b < m; ++b) Sa[b] += ya * y[b];
+            }
         }
+    }
+    for (int a = 0; a < m; ++a)
+        for (int b = 0; b < a; ++b) S[(size_t)a * m + b] = S[(size_t)b * m + a];
     std::vector<double> rs(m, 0.0);
     double tot = 0;
     for (int a = 0; a < m; ++a) {
@@ -420,7 +553,9 @@ extern "C" int or_extract(const double* X, const int32_t* labels, double* C, int
         if (counts[j]) ++sum_class;
     }
     const int Fal = mode == OR_MODE_COMPAT ? or_fft_size(m, OR_MODE_COMPAT) : or_fft_size(m, OR_MODE_CANONICAL);
-    std::vector<double> ncc(2 * m - 1);
+    // per non-empty cluster: the centred Gram M and the sign reference a, kept for
+    // the eigenvector phase, which runs the clusters in parallel
+    std::vector<std::vector<double>> Ms(k), As(k);
     for (int j = 0; j < k; ++j) {
         int cnt = counts[j];
         double* cj = C + (int64_t)j * m;
@@ -448,7 +583,10 @@ extern "C" int or_extract(const double* X, const int32_t* labels, double* C, int
             gate = s != 0;
         }
         if (gate) {
-            std::vector<double> tmp(m);
+#pragma omp parallel
+            {
+            std::vector<double> tmp(m), ncc(2 * m - 1);
+#pragma omp for schedule(dynamic, 64)
             for (int i = 0; i < cnt; ++i) {
                 double* row = &Y[(size_t)i * m];
                 int shift;
@@ -461,6 +599,7 @@ extern "C" int or_extract(const double* X, const int32_t* labels, double* C, int
                 zero_shift(row, tmp.data(), shift, m);
                 std::memcpy(row, tmp.data(), sizeof(double) * m);
             }
+            }
         }
         std::vector<double> a(m);
         if (mode == OR_MODE_PYREF) {
@@ -470,8 +609,16 @@ extern "C" int or_extract(const double* X, const int32_t* labels, double* C, int
             or_znorm(Y.data(), cnt, m, 1);                      // z_norm_gpu_x(seg, ddof=1) (:1141)
             std::memcpy(a.data(), &Y[0], sizeof(double) * m);  // val_copy: first member (:192-200)
         }
-        std::vector<double> M;
-        gram_centered(Y, cnt, m, M);
+        gram_centered(Y, cnt, m, Ms[j]);
+        As[j] = std::move(a);
+    }
+    // eigenvector, sign rule and store of every non-empty cluster (independent)
+#pragma omp parallel for schedule(dynamic, 1)
+    for (int j = 0; j < k; ++j) {
+        if (counts[j] == 0) continue;
+        double* cj = C + (int64_t)j * m;
+        const std::vector<double>& M = Ms[j];
+        std::vector<double>& a = As[j];
         std::vector<double> v(m), w(m);
         if (mode == OR_MODE_COMPAT) {
             if (cal_select) {  // get_class_centers_a: syevd top eigenvector (:367-468)
@@ -681,4 +828,12 @@ extern "C" double or_ari(const int32_t* a, const int32_t* b, int64_t n) {
     double mx = 0.5 * (sa + sb);
     if (mx == expected) return 1.0;
     return (sij - expected) / (mx - expected);
+}
+
+// The engine's synthetic workloads (gen_core.h), so that the CPU baseline runs on
+// the same series without loading the engine's library.
+extern "C" int or_generate(int64_t n, int m, int classes, double noise, double dirichlet, uint64_t seed,
+                           float* data, int32_t* labels) {
+    const tcgen::Params p{n, m, classes, noise, dirichlet, seed};
+    return tcgen::generate(&p, data, labels) ? 0 : 1;
 }

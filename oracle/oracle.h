@@ -111,6 +111,11 @@ double or_ari(const int32_t* a, const int32_t* b, int64_t n);
 /* Label parsing of the reference: k from labels (test_kshape.cu:24-30). */
 int or_k_from_labels(const int32_t* labels, int64_t n);
 
+// The engine's synthetic workloads (times-c_gb300/csrc/gen_core.h): data n*m,
+// labels n (may be null).  Returns 0, or 1 for invalid parameters.
+int or_generate(int64_t n, int m, int classes, double noise, double dirichlet, uint64_t seed, float* data,
+                int32_t* labels);
+
 #ifdef __cplusplus
 }
 #endif

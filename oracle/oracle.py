@@ -65,6 +65,9 @@ def lib():
         L.or_ari.argtypes = [_i32p, _i32p, _i64]
         L.or_k_from_labels.restype = _int
         L.or_k_from_labels.argtypes = [_i32p, _i64]
+        L.or_generate.restype = _int
+        L.or_generate.argtypes = [_i64, _int, _int, ctypes.c_double, ctypes.c_double, ctypes.c_uint64,
+                                  _fp, _i32p]
         _lib = L
     return _lib
 
@@ -174,3 +177,13 @@ def kshape(data, k, mode, init_labels, init_chose=0, seed=0, max_iter=10, restar
         raise ValueError("oracle kshape rejected the job")
     return dict(labels=labels, centroids=cents, iterations=res.iterations, sum_class=res.sum_class,
                 restarted=res.restarted, inertia=res.inertia, min_margin=res.min_margin)
+
+
+def generate(n, m, classes, noise=0.2, dirichlet=0.0, seed=0):
+    """The engine's synthetic series (n x m float32) and class labels, made by the
+    oracle library from the same generator source, without the engine's library."""
+    data = np.empty((n, m), np.float32)
+    labels = np.empty(n, np.int32)
+    if lib().or_generate(n, m, classes, noise, dirichlet, seed, data.ctypes.data_as(_fp), _i(labels)) != 0:
+        raise ValueError("generate: invalid parameters")
+    return data, labels

@@ -3,11 +3,16 @@ FP64 oracle on the same inputs.
 
 Tolerances (FP32 kernels vs the FP64 restatement):
   z-norm values           abs 2e-6
-  SBD distances           abs 2e-5
+  SBD distances           abs 2e-6 (m <= 1024), 1e-5 (longer series)
   labels                  identical wherever the oracle's best-vs-second margin
-                          exceeds 1e-4 (below that FP32 rounding may pick either)
-  shifts                  identical, or the GPU lag's NCC within 2e-5 of the max
-  centroids               max abs error 1e-4 per unit-norm vector
+                          exceeds 1e-5 (five times the distance tolerance: below
+                          that FP32 rounding may pick either); the number of
+                          series under the margin is printed
+  shifts                  identical, or the GPU lag's NCC within 2e-6 of the max
+  centroids               1e-5 relative: max |c - c_oracle| <= 1e-5 max |c_oracle|
+  whole loops             labels identical when no assignment of the oracle's run
+                          came within 1e-5 of a tie; otherwise ARI >= 0.99, and the
+                          test prints that the fallback was taken
 """
 import os
 import subprocess
@@ -17,7 +22,12 @@ import pytest
 
 pytestmark = pytest.mark.gpu
 
-MARGIN = 1e-4
+MARGIN = 1e-5
+CENTROID_REL = 1e-5
+
+
+def dist_tol(m):
+    return 2e-6 if m <= 1024 else 1e-5
 
 
 @pytest.fixture(scope="module")
@@ -64,15 +74,18 @@ def test_init_labels_deterministic(gpu_ctx):
 def _check_assign(O, X, C, F, labels, dist, shift, clamp2, tag):
     ol, od, osh, om = O.assign(X, C, F, clamp2=clamp2)
     clear = om > MARGIN
-    assert np.array_equal(labels[clear], ol[clear]), (tag, np.flatnonzero((labels != ol) & clear)[:10])
-    np.testing.assert_allclose(dist[clear], od[clear], atol=2e-5, err_msg=tag)
-    # shift: same lag, or a lag whose NCC is within 2e-5 of the max
     m = X.shape[1]
+    derr = float(np.abs(dist[clear] - od[clear]).max()) if clear.any() else 0.0
+    print("%s: %d of %d series within %.0e of a tie, labels differ elsewhere %d, max distance error %.2e"
+          % (tag, int((~clear).sum()), len(labels), MARGIN, int((labels != ol)[clear].sum()), derr))
+    assert np.array_equal(labels[clear], ol[clear]), (tag, np.flatnonzero((labels != ol) & clear)[:10])
+    assert derr <= dist_tol(m), (tag, derr)
+    # shift: same lag, or a lag whose NCC is within the distance tolerance of the max
     bad = 0
     for i in np.flatnonzero(clear & (shift != osh)):
         c = C[ol[i]]
         ncc_align = O.ncc(c, X[i], F)  # NCC(center, member): slot j <-> shift j - m + 1
-        if ncc_align.max() - ncc_align[shift[i] + m - 1] > 2e-5:
+        if ncc_align.max() - ncc_align[shift[i] + m - 1] > dist_tol(m):
             bad += 1
     assert bad == 0, (tag, bad)
 
@@ -135,9 +148,9 @@ def test_extract_shapes(gpu_ctx, mods, mode, m, k, n, cinit):
     assert sc == refsc
     np.testing.assert_array_equal(counts.cpu().numpy(), refcnt)
     got = c.cpu().numpy()
-    scale = 1.0 if mode == 0 else np.sqrt(m)  # canonical centroids are z-normalised
-    err = np.abs(got - refC).max(axis=1) / scale
-    assert err.max() < 1e-4, err
+    rel = float(np.abs(got - refC).max() / np.abs(refC).max())
+    print("extract m=%d k=%d mode=%d start=%s: centroid error %.2e relative" % (m, k, mode, cinit, rel))
+    assert rel <= CENTROID_REL, rel
 
 
 @pytest.mark.parametrize("prec,tol", [(2, 2e-3), (1, 1e-2)])
@@ -192,12 +205,16 @@ def test_kshape_loop_matches_oracle(gpu_ctx, mods, mode, init_chose, seed):
     g = gpu_ctx.kshape_run(data, 4, mode=mode, init_chose=init_chose, seed=seed, max_iter=100)
     o = O.kshape(data, 4, mode, init, init_chose=init_chose, seed=seed, max_iter=100)
     assert g["restarted"] == o["restarted"]
+    rel = float(np.abs(g["centroids"] - o["centroids"]).max() / np.abs(o["centroids"]).max())
+    print("loop mode=%d init=%d seed=%d: oracle min margin %.1e, labels differ %d, centroid error %.2e relative"
+          % (mode, init_chose, seed, o["min_margin"], int((g["labels"] != o["labels"]).sum()), rel))
     if o["min_margin"] > MARGIN:
         np.testing.assert_array_equal(g["labels"], o["labels"])
         assert g["iterations"] == o["iterations"] and g["sum_class"] == o["sum_class"]
-        scale = 1.0 if mode == 0 else np.sqrt(128)
-        assert np.abs(g["centroids"] - o["centroids"]).max() / scale < 1e-4
+        assert rel <= CENTROID_REL, rel
     else:
+        print("  fallback taken: the oracle's run came within %.0e of a tie; ARI %.4f"
+              % (MARGIN, O.ari(g["labels"], o["labels"])))
         assert O.ari(g["labels"], o["labels"]) >= 0.99
 
 
@@ -230,6 +247,7 @@ def test_cli_labeled_file(gpu_ctx, mods, tmp_path):
     if o["min_margin"] > MARGIN:
         np.testing.assert_array_equal(labels, o["labels"])
     else:
+        print("cli: fallback taken (oracle min margin %.1e)" % o["min_margin"])
         assert O.ari(labels, o["labels"]) >= 0.99
     C, _ = T.read_file(str(cen), False)
     assert C.shape == (4, 128)

@@ -1,0 +1,119 @@
+"""The FP64 oracle against the reference's own GPU build (CPU only).
+
+tests/golden/ref_gpu_golden.npz and ref_gpu_c2.npz hold outputs of the
+reference's CUDA code compiled for sm_103a and run on a GB300 by
+tests/golden/make_ref_gpu_golden.py.  These tests pin the oracle's compat
+semantics - wrap-around lag slots (ncc.cuh:230-245), pad-with-2
+(kshape.cuh:55-60), the int-truncating alignment gate (shapeExtract.cuh:1131),
+m power steps (:590-606) and the syevd path (:367-468, :649-692) - on the
+reference's own results, and record where the reference's results are not a
+function of its inputs.
+"""
+import hashlib
+import os
+
+import numpy as np
+import pytest
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+GOLDEN = os.path.join(HERE, "golden", "ref_gpu_golden.npz")
+GOLDEN_C2 = os.path.join(HERE, "golden", "ref_gpu_c2.npz")
+CASES = ["c1", "w100", "w129", "w300", "w512"]
+CLEAN = ["w129", "w300", "w512"]
+
+
+@pytest.fixture(scope="module")
+def gold():
+    return np.load(GOLDEN)
+
+
+def _meta(g, name):
+    return tuple(int(v) for v in g[name + "__meta"])
+
+
+@pytest.mark.parametrize("name", CASES)
+@pytest.mark.parametrize("cents", ["ext", "raw"])
+def test_oracle_assign_matches_reference_gpu(built, gold, name, cents):
+    _, O = built
+    n, m, k, _ = _meta(gold, name)
+    xz = gold[name + "__xz"].astype(np.float64)
+    C = gold[name + "__extract_zero_cal0__centroids"] if cents == "ext" else gold[name + "__x"][gold[name + "__raw_rows"]]
+    lab, dist, _, _ = O.assign(xz, C.astype(np.float64), O.fft_size(m, O.MODE_COMPAT), clamp2=True)
+    assert np.array_equal(lab, gold["%s__assign_%s__labels" % (name, cents)] - 1)
+    assert np.abs(dist - gold["%s__assign_%s__dist" % (name, cents)]).max() <= 1e-6
+
+
+@pytest.mark.parametrize("name", CLEAN)
+def test_oracle_znorm_matches_reference_gpu(built, gold, name):
+    _, O = built
+    z = O.znorm(gold[name + "__x"].astype(np.float64))
+    assert np.abs(z - gold[name + "__znorm"]).max() <= 2e-6
+
+
+@pytest.mark.parametrize("name", ["c1", "w100"])
+def test_reference_znorm_reads_an_unset_slot(built, gold, name):
+    """normalization.cuh:36-39 leaves sh_row[m] unwritten for m < 1024; on the GB300
+    it held non-zero data at these lengths, so some rows were scaled by a wrong
+    standard deviation (or became NaN).  Parity at these lengths covers only the
+    scale-invariant assignment."""
+    _, O = built
+    z = O.znorm(gold[name + "__x"].astype(np.float64))
+    zr = gold[name + "__znorm"].astype(np.float64)
+    with np.errstate(invalid="ignore"):
+        off = ~np.all(np.abs(zr - z) <= 1e-5, axis=1)
+    assert off.sum() >= 10
+
+
+@pytest.mark.parametrize("name", CLEAN)
+@pytest.mark.parametrize("start", ["zero", "raw", "unit"])
+@pytest.mark.parametrize("cal", [0, 1])
+def test_oracle_extract_matches_reference_gpu(built, gold, name, start, cal):
+    _, O = built
+    n, m, k, _ = _meta(gold, name)
+    C0 = {"zero": np.zeros((k, m)), "raw": gold[name + "__x"][gold[name + "__raw_rows"]],
+          "unit": gold[name + "__unit"]}[start].astype(np.float64)
+    C, counts, sc = O.extract(gold[name + "__xz"].astype(np.float64), gold[name + "__truth"].astype(np.int32), C0,
+                              O.MODE_COMPAT, cal)
+    key = "%s__extract_%s_cal%d" % (name, start, cal)
+    Cr = gold[key + "__centroids"].astype(np.float64)
+    assert np.array_equal(counts, gold[key + "__counts"])
+    assert sc == int(gold[key + "__sum_class"][0])
+    assert np.abs(C - Cr).max() <= 1e-5 * np.abs(Cr).max()
+
+
+@pytest.mark.parametrize("name", CLEAN)
+@pytest.mark.parametrize("init_chose,seed", [(0, 0), (1, 0), (1, 1)])
+def test_oracle_loop_matches_reference_gpu(built, gold, name, init_chose, seed):
+    _, O = built
+    n, m, k, cap = _meta(gold, name)
+    init = gold[name + "__init"] - 1  # the reference's curand labels (also the restart's start)
+    o = O.kshape(gold[name + "__x"], k, O.MODE_COMPAT, init, init_chose=init_chose, seed=seed, max_iter=cap)
+    key = "%s__loop_i%d_s%d" % (name, init_chose, seed)
+    _, sum_class, restarted = (int(v) for v in gold[key + "__info"])
+    assert np.array_equal(o["labels"], gold[key + "__labels"] - 1)
+    assert o["sum_class"] == sum_class and o["restarted"] == restarted
+
+
+def test_reference_not_reproducible_above_1024(built):
+    """At m = 2709 the reference's norm_vec rescales each power-iteration vector from
+    three 1024-thread blocks while the others still read it (shapeExtract.cuh:
+    287-323, SURVEY's inter-block race): two runs of its extraction on the same
+    input disagree, and so do two runs of its whole init_chose=0 loop."""
+    g = np.load(GOLDEN_C2)
+    a, b = g["extract_zero_cal0_run0"], g["extract_zero_cal0_run1"]
+    assert np.abs(a - b).max() > 1e-2
+    assert not np.array_equal(g["labels_init0_run_a"], g["labels_init0_run_b"])
+
+
+def test_oracle_c2_init1_matches_reference_gpu(built):
+    """n = 20,000, m = 2709, k = 8, init_chose=1 seed 1: the reference stops after one
+    assignment against raw rows (<= k/2 clusters keep members); the oracle's loop
+    gives the same labels."""
+    _, O = built
+    g = np.load(GOLDEN_C2)
+    x, _ = O.generate(20000, 2709, 8, noise=0.2, dirichlet=2.0, seed=1)
+    if hashlib.sha256(x.tobytes()).digest() != bytes(g["x_sha256"]):
+        pytest.skip("the generator gives other series on this host than where the reference ran")
+    o = O.kshape(x, 8, O.MODE_COMPAT, g["init"] - 1, init_chose=1, seed=1, max_iter=20)
+    assert np.array_equal(o["labels"], g["labels_init1"] - 1)
+    assert o["sum_class"] == int(g["info_init1"][1])

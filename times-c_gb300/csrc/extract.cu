@@ -386,8 +386,9 @@ void extract_async(tc_ctx* ctx, const ExtractArgs& a, cudaStream_t s) {
     TC_CHECK_LAUNCH();
 
     // power iteration: compat runs at most m steps (the reference's fixed count),
-    // stopping early once every cluster's step difference is at FP32 noise level;
-    // cal_select=1 / canonical converge fully (the reference's syevd result).
+    // stopping early only once a cluster's vector will move by less than 3e-8 in the
+    // steps left (geometric tail of the measured contraction) or has reached rounding
+    // level; cal_select=1 / canonical converge fully (the reference's syevd result).
     const bool full = a.cal_select || a.mode == TC_MODE_CANONICAL;
     const int tmax = full ? std::max(4 * m, 200) : m;
     const double tol = full ? 5e-7 : 1e-6;

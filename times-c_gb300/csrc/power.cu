@@ -47,7 +47,8 @@ struct PowerClusterParams {
     int lead_rows;
     float* C;
     int k, m, tmax, mode;
-    double tol2;
+    double tol2;   // squared step difference below which the stop test applies
+    double tail2;  // squared bound on the movement still to come (geometric tail)
     int* steps;  // per cluster: the step T whose vector was stored (diagnostics)
     // start vectors from the repeated squaring (k x ld, any scale) where vok[c];
     // such clusters run at most tmax_sq steps
@@ -107,7 +108,8 @@ __global__ void __launch_bounds__(PC_THREADS, 1) k_power_cluster(PowerClusterPar
     const double* rc = p.r + (size_t)c * m;
     const float* Sc = p.S + (size_t)c * m * ld;
     const double inv_m = 1.0 / (double)m, totc = p.tot[c];
-    const float finv_m = (float)inv_m, totf = (float)totc, tol2f = (float)p.tol2;
+    const float finv_m = (float)inv_m, totf = (float)totc, tol2f = (float)p.tol2, tail2f = (float)p.tail2;
+    float ddp = 0.f;  // the previous step's squared difference (warp 0, lane 0)
     for (int i = threadIdx.x; i < nrow; i += PC_THREADS) r_own[i] = (float)rc[a0 + i];
     const int nv4 = ld / 4;
     float4* srows = reinterpret_cast<float4*>(r_own + a16((size_t)nrow * 4) / 4);
@@ -307,7 +309,22 @@ __global__ void __launch_bounds__(PC_THREADS, 1) k_power_cluster(PowerClusterPar
                 sh_corr[0] = -sv * finv_m;
                 sh_corr[1] = fmaf(totf * finv_m * finv_m, sv, -rv * finv_m);
                 sh_inv = inv;
-                sh_done = t >= tmax || (t >= 1 && dd < tol2f) || !(n2 > 0.f);
+                // Stop test, once the step difference d_t = |v_t - v_{t-1}| is below tol:
+                // the iteration contracts by rho = d_t/d_{t-1} per step, so the movement
+                // still to come is about d_t rho/(1 - rho); stop when that is below the
+                // tail bound, or when d_t no longer shrinks (rounding level).  A cluster
+                // whose top eigenvalues nearly tie (rho near 1) runs on towards tmax.
+                bool conv = false;
+                if (t >= 2 && dd < tol2f) {
+                    if (!(dd < ddp)) {
+                        conv = true;
+                    } else {
+                        const float r = sqrtf(dd / ddp), q = 1.f - r;
+                        conv = dd * r * r < tail2f * q * q;
+                    }
+                }
+                ddp = dd;
+                sh_done = t >= tmax || conv || !(n2 > 0.f);
             }
         }
         __syncthreads();
@@ -419,8 +436,9 @@ void power_eigvecs(tc_ctx* ctx, const float* S, int ld, const double* r, const d
                    const int32_t* offsets, const float* seg, bool lead_rows, int k, int m, int mode, int tmax,
                    double tol, const float* vinit, const int32_t* vok, int tmax_sq, float* C, cudaStream_t s) {
     int* steps = ctx->ws.pstats.as<int>((size_t)k);
-    PowerClusterParams pp{S,  ld, r,  tot,        counts, offsets, seg,   lead_rows ? 1 : 0, C, k, m, tmax, mode,
-                          tol * tol, steps, vinit, vok, tmax_sq};
+    const double tail = 3e-8;  // movement still to come, L2 norm of a unit vector
+    PowerClusterParams pp{S,     ld,          r,     tot,   counts, offsets, seg,  lead_rows ? 1 : 0, C, k, m, tmax,
+                          mode,  tol * tol,   tail * tail,  steps,  vinit,   vok,  tmax_sq};
     // long series stream tens of MB per step from HBM: spread each over 16 SMs
     if (m > 1024) {
         const size_t smem = cluster_smem<16>(m, ld, false);
