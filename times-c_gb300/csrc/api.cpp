@@ -51,10 +51,25 @@ static void check_shape(int64_t n, int m, int k, int mode) {
                "FFT length " + std::to_string(F) + " outside [8, 16384] (series too short or too long for this mode)");
 }
 
-// One assignment against the current centroids.
-static void assign(tc_ctx* ctx, const float* x, const float* C, int64_t n, int m, int k, int mode, int precision,
-                   int32_t* labels, float* dist, int32_t* shift, const int32_t* old, int32_t* changed,
-                   double* dsum, cudaStream_t s) {
+// The bounded assignment across iterations (FP32 form, at the lengths the tensor-core
+// screen takes): lower bounds on every (series, centroid) distance, carried from one
+// assignment to the next with each centroid's movement, let the FFT pass skip the
+// pairs that cannot be a series' first minimum.  Bounds are kept only for series that
+// stay fixed across calls - those prepared by tc_prepare_series (or the whole loop's
+// own normalised copy) - and are rebuilt by the screened pass whenever the bounded
+// pass had to evaluate more than BOUNDS_REFRESH_FRACTION of the pairs.
+enum { BOUNDS_OFF = 0, BOUNDS_AUTO = -1, BOUNDS_REFRESH = 1, BOUNDS_USE = 2 };
+constexpr double BOUNDS_REFRESH_FRACTION = 0.3;
+
+static bool bounds_usable(const tc_ctx* ctx, const float* x, int64_t n, int m, int k, int mode, int precision) {
+    return precision == TC_PREC_FP32 && screen_supported(m, fft_size(m, mode), k) && !std::getenv("TIMESC_NO_BOUNDS") &&
+           ctx->prep_x == x && ctx->prep_n == n && ctx->prep_m == m;
+}
+
+// One assignment against the current centroids.  Returns the bounds mode it ran.
+static int assign(tc_ctx* ctx, const float* x, const float* C, int64_t n, int m, int k, int mode, int precision,
+                  int32_t* labels, float* dist, int32_t* shift, const int32_t* old, int32_t* changed,
+                  double* dsum, cudaStream_t s, int bmode = BOUNDS_AUTO) {
     const int F = fft_size(m, mode);
     AssignArgs a{};
     a.x = x;
@@ -70,21 +85,64 @@ static void assign(tc_ctx* ctx, const float* x, const float* C, int64_t n, int m
     a.changed = changed;
     a.dist_sum = dsum;
     if (precision == TC_PREC_FP32 && !shift && screen_supported(m, F, k)) {
+        Workspace& ws = ctx->ws;
+        BoundsState& b = ctx->bounds;
+        const bool usable = bmode != BOUNDS_OFF && bounds_usable(ctx, x, n, m, k, mode, precision);
+        if (usable && !(b.x == x && b.n == n && b.m == m && b.k == k && b.mode == mode)) {
+            b = BoundsState{};
+            b.x = x;
+            b.n = n;
+            b.m = m;
+            b.k = k;
+            b.mode = mode;
+        }
+        int use = BOUNDS_OFF;
+        if (usable) use = bmode == BOUNDS_AUTO ? (b.valid && !b.refresh ? BOUNDS_USE : BOUNDS_REFRESH) : bmode;
+        if (use == BOUNDS_USE && !b.valid) use = BOUNDS_REFRESH;
+        float *lb = nullptr, *delta = nullptr;
+        unsigned long long* evals = reinterpret_cast<unsigned long long*>(ws.aux.as<char>(64) + 24);
+        if (use != BOUNDS_OFF) {
+            lb = ws.bounds.as<float>((size_t)2 * k * n);
+            float* cprev = ws.cprev.as<float>((size_t)k * m + k);
+            delta = cprev + (size_t)k * m;
+            launch_centroid_delta(C, k, m, cprev, delta, s);  // cprev <- these centroids
+            a.lb_eps = (float)(fft_error(m, F) + 1e-6);
+            TC_CUDA(cudaMemsetAsync(evals, 0, sizeof(unsigned long long), s));
+        }
+        float2* spec = ws.spectra.as<float2>((size_t)k * (F / 2 + 1));
+        launch_centroid_spectra(ctx, C, k, m, F, spec, s);
+        a.spec = spec;
+        if (use == BOUNDS_USE) {
+            a.lb_in = lb;
+            a.lb_out = lb + (size_t)k * n;
+            a.delta = delta;
+            a.evals = evals;
+            launch_assign_fft(ctx, a, s);
+            TC_CUDA(cudaMemcpyAsync(lb, lb + (size_t)k * n, sizeof(float) * k * n, cudaMemcpyDeviceToDevice, s));
+            return use;
+        }
         // exact screening: the BF16 pass keeps every centroid whose FP32 distance can be
         // the minimum, the FP32 pass evaluates those (same labels and distances as the
-        // unscreened FP32 kernel)
+        // unscreened FP32 kernel); with bounds, both write theirs for every pair
         a.centroids = C;
-        a.cand = ctx->ws.screen.as<int32_t>((size_t)n * (SCREEN_CAP + 1));
+        a.cand = ws.screen.as<int32_t>((size_t)n * (SCREEN_CAP + 1));
         a.ncand = a.cand + (size_t)n * SCREEN_CAP;
+        if (use == BOUNDS_REFRESH) {
+            a.lb_out = lb;
+            a.lb_d16 = (float)bf16_error(m, F);
+        }
         // -1 (all centroids) for every series the tensor-core pass does not reach,
         // e.g. after one of its bounded waits ran out
         TC_CUDA(cudaMemsetAsync(a.ncand, 0xFF, (size_t)n * sizeof(int32_t), s));
         launch_assign_tc(ctx, a, TC_PREC_BF16, s);
-        float2* spec = ctx->ws.spectra.as<float2>((size_t)k * (F / 2 + 1));
-        launch_centroid_spectra(ctx, C, k, m, F, spec, s);
-        a.spec = spec;
         launch_assign_fft(ctx, a, s);
-    } else if (precision == TC_PREC_FP32 || shift || !tc_assign_supported(m, F, k, precision)) {
+        if (use == BOUNDS_REFRESH) {
+            b.valid = true;
+            b.refresh = false;
+        }
+        return use;
+    }
+    if (precision == TC_PREC_FP32 || shift || !tc_assign_supported(m, F, k, precision)) {
         float2* spec = ctx->ws.spectra.as<float2>((size_t)k * (F / 2 + 1));
         launch_centroid_spectra(ctx, C, k, m, F, spec, s);
         a.spec = spec;
@@ -92,6 +150,20 @@ static void assign(tc_ctx* ctx, const float* x, const float* C, int64_t n, int m
     } else {
         a.centroids = C;
         launch_assign_tc(ctx, a, precision, s);
+    }
+    return BOUNDS_OFF;
+}
+
+// After an assignment that kept bounds: count it, and after a bounded pass rebuild
+// the bounds next time if it evaluated too many pairs.
+static void bounds_feedback(tc_ctx* ctx, int used, unsigned long long evals, int64_t n, int k) {
+    BoundsState& b = ctx->bounds;
+    if (used == BOUNDS_REFRESH) {
+        ++b.screened;
+    } else if (used == BOUNDS_USE) {
+        ++b.bounded;
+        b.bounded_pairs += evals;
+        b.refresh = (double)evals > BOUNDS_REFRESH_FRACTION * (double)n * k;
     }
 }
 
@@ -213,11 +285,13 @@ static LoopState run_loop(tc_ctx* ctx, const tc_job* job, const float* x, int k,
         int32_t pad;
         double dsum;
         int32_t sum_class, bad_label;
-        int32_t pad2[6];
+        unsigned long long evals;  // pairs the bounded pass evaluated (+24)
+        int32_t pad2[4];
         int32_t err[2];
     } h;
     static_assert(sizeof(h) == 56, "aux layout");
-    StageGraph g_extract, g_assign;
+    StageGraph g_extract, g_assign, g_assign_bounded;
+    const bool bnd = bounds_usable(ctx, x, n, m, k, job->mode, job->precision);
     const bool graphs = ctx->graphs && !std::getenv("TIMESC_NO_GRAPHS");
     auto readback = [&]() {
         TC_CUDA(cudaMemcpyAsync(&h, aux, sizeof(h), cudaMemcpyDeviceToHost, s));
@@ -225,10 +299,10 @@ static LoopState run_loop(tc_ctx* ctx, const tc_job* job, const float* x, int k,
         check_async_errors(h.err);
     };
     TC_CUDA(cudaMemsetAsync(aux, 0, 64, s));
-    auto issue_assign = [&]() {
+    auto issue_assign = [&](int bmode) {
         TC_CUDA(cudaMemsetAsync(aux, 0, 16, s));
         // no shifts here: the extraction computes its own where the gate is open
-        assign(ctx, x, C, n, m, k, job->mode, job->precision, labels, dist, nullptr, old, changed, dsum, s);
+        assign(ctx, x, C, n, m, k, job->mode, job->precision, labels, dist, nullptr, old, changed, dsum, s, bmode);
     };
     ExtractArgs e{};
     e.x = x;
@@ -247,8 +321,19 @@ static LoopState run_loop(tc_ctx* ctx, const tc_job* job, const float* x, int k,
         TC_CUDA(cudaMemcpyAsync(aux + 16, ws.scal.p, 2 * sizeof(int32_t), cudaMemcpyDeviceToDevice, s));
     };
     auto do_assign = [&]() -> bool {
-        g_assign.run(graphs, s, issue_assign);
+        // the bounded pass while the bounds are valid and last pass evaluated few pairs;
+        // the screened pass (rebuilding the bounds) otherwise - one graph for each
+        const bool use_b = bnd && ctx->bounds.valid && !ctx->bounds.refresh;
+        if (use_b) g_assign_bounded.run(graphs, s, [&]() { issue_assign(BOUNDS_USE); });
+        else g_assign.run(graphs, s, [&]() { issue_assign(BOUNDS_REFRESH); });
         readback();
+        if (bnd) {
+            if (!use_b) {
+                ctx->bounds.valid = true;
+                ctx->bounds.refresh = false;
+            }
+            bounds_feedback(ctx, use_b ? BOUNDS_USE : BOUNDS_REFRESH, h.evals, n, k);
+        }
         check_guards(ctx, "assignment");
         st.inertia = h.dsum / (double)n;
         return h.changed == 0;
@@ -297,7 +382,8 @@ static LoopState run_loop(tc_ctx* ctx, const tc_job* job, const float* x, int k,
 static const char* const WS_NAMES[] = {"x", "labels", "old_labels", "shift", "dist", "centroids", "spectra",
                                        "seg", "perm", "chunk_counts", "counts", "offsets", "gate", "scal",
                                        "gram", "rowsum", "gram_yt", "gram_poff", "piter", "pstats", "aux",
-                                       "toeplitz", "toeplitz_norm", "xbf", "xbf_norm", "first", "gram_sq", "sq_meta", "screen", "gram_part"};
+                                       "toeplitz", "toeplitz_norm", "xbf", "xbf_norm", "first", "gram_sq", "sq_meta", "screen", "gram_part",
+                                       "bounds", "cprev"};
 
 static std::vector<DevBuf*> workspace_buffers(tc_ctx* ctx);
 
@@ -333,12 +419,14 @@ static std::vector<DevBuf*> workspace_buffers(tc_ctx* ctx) {
     return {&w.x,    &w.labels,  &w.old_labels, &w.shift,   &w.dist,      &w.centroids, &w.spectra,
             &w.seg,  &w.perm,    &w.chunk_counts, &w.counts, &w.offsets,  &w.gate,      &w.scal,
             &w.gram, &w.rowsum,  &w.gram_yt,    &w.gram_poff, &w.piter,   &w.pstats,    &w.aux,
-            &w.toeplitz, &w.toeplitz_norm, &w.xbf, &w.xbf_norm, &w.first, &w.gram_sq, &w.sq_meta, &w.screen, &w.gram_part};
+            &w.toeplitz, &w.toeplitz_norm, &w.xbf, &w.xbf_norm, &w.first, &w.gram_sq, &w.sq_meta, &w.screen, &w.gram_part,
+            &w.bounds, &w.cprev};
 }
 
 void release_workspace(tc_ctx* ctx) {
     for (DevBuf* b : workspace_buffers(ctx)) b->release();
     ctx->prep_x = nullptr;
+    ctx->bounds.valid = false;
 }
 
 size_t workspace_bytes(tc_ctx* ctx) {
@@ -456,18 +544,32 @@ int tc_sbd_assign(tc_ctx* ctx, const float* d_x, const float* d_centroids, int64
     TC_REQUIRE(precision >= TC_PREC_FP32 && precision <= TC_PREC_TF32, TC_ERR_ARG, "unknown precision");
     TC_CUDA(cudaSetDevice(ctx->device));
     cudaStream_t s = (cudaStream_t)stream;
-    int* words = reinterpret_cast<int*>(ctx->ws.aux.as<char>(64) + 48);
-    TC_CUDA(cudaMemsetAsync(words, 0, 2 * sizeof(int), s));
-    assign(ctx, d_x, d_centroids, n, m, k, mode, precision, d_labels, d_dist, d_shift, d_old_labels, d_changed,
-           d_dist_sum, s);
+    char* aux = ctx->ws.aux.as<char>(64);
+    TC_CUDA(cudaMemsetAsync(aux + 48, 0, 2 * sizeof(int), s));
+    const int used = assign(ctx, d_x, d_centroids, n, m, k, mode, precision, d_labels, d_dist, d_shift,
+                            d_old_labels, d_changed, d_dist_sum, s);
     const bool tc_used = precision != TC_PREC_FP32 || (!d_shift && screen_supported(m, fft_size(m, mode), k));
-    if (tc_used) {  // the tensor-core pass reports through an error word
-        int h[2] = {0, 0};
-        TC_CUDA(cudaMemcpyAsync(h, words, sizeof(h), cudaMemcpyDeviceToHost, s));
+    if (tc_used) {  // the tensor-core pass reports through an error word; the bounded pass counts its pairs
+        struct {
+            unsigned long long evals;
+            int32_t pad[4];
+            int32_t err[2];
+        } h;
+        static_assert(sizeof(h) == 32, "aux layout");
+        TC_CUDA(cudaMemcpyAsync(&h, aux + 24, sizeof(h), cudaMemcpyDeviceToHost, s));
         TC_CUDA(cudaStreamSynchronize(s));
-        check_async_errors(h);
+        check_async_errors(h.err);
+        bounds_feedback(ctx, used, h.evals, n, k);
     }
     TC_API_END(ctx)
+}
+
+int tc_assign_stats(const tc_ctx* ctx, uint64_t* screened, uint64_t* bounded, uint64_t* bounded_pairs) {
+    if (!ctx) return TC_ERR_ARG;
+    if (screened) *screened = ctx->bounds.screened;
+    if (bounded) *bounded = ctx->bounds.bounded;
+    if (bounded_pairs) *bounded_pairs = ctx->bounds.bounded_pairs;
+    return TC_OK;
 }
 
 int tc_prepare_series(tc_ctx* ctx, const float* d_x, int64_t n, int m, tc_stream stream) {

@@ -106,7 +106,7 @@ __device__ __forceinline__ double team_sum(float x, int team, int tid, TeamScrat
     return v;
 }
 
-// (val, u) max over the team (larger u wins ties); valid on tid 0.
+// (val, u) max over the team (larger u wins ties); every thread of the team gets it.
 template <int T>
 __device__ __forceinline__ LagMax team_max(LagMax lm, int team, int tid, TeamScratch* scr) {
     constexpr int W = T < 32 ? T : 32;
@@ -122,8 +122,9 @@ __device__ __forceinline__ LagMax team_max(LagMax lm, int team, int tid, TeamScr
             scr->u[tid >> 5] = lm.u;
         }
         team_sync<T>(team);
-        if (tid == 0)
-            for (int w = 1; w < T / 32; ++w) lm.take(scr->val[w], scr->u[w]);
+        lm.val = scr->val[0];
+        lm.u = scr->u[0];
+        for (int w = 1; w < T / 32; ++w) lm.take(scr->val[w], scr->u[w]);
     }
     return lm;
 }
@@ -226,6 +227,12 @@ struct AssignParams {
     // screened assignment: only centroids cand[i][0 .. ncand[i]) (ascending; -1: all)
     const int32_t* cand;
     const int32_t* ncand;
+    // lower bounds [k][n] on the exact distances (see launch_assign_fft)
+    float* lb_out;
+    const float* lb_in;
+    const float* delta;
+    float lb_eps;
+    unsigned long long* evals;
 };
 
 // Max NCC over the valid lags with the lag of the first maximum in sbd3D's order
@@ -255,7 +262,7 @@ struct MaxOut {
     }
 };
 
-template <int N, bool CSMEM, bool SHIFT>
+template <int N, bool CSMEM, bool SHIFT, bool BOUNDED>
 __global__ void __launch_bounds__(Cfg<N>::BLOCK, 1) k_assign_fft(AssignParams p) {
     typedef Core<N> Co;
     constexpr int T = Co::T, TEAMS = Cfg<N>::TEAMS;
@@ -276,6 +283,7 @@ __global__ void __launch_bounds__(Cfg<N>::BLOCK, 1) k_assign_fft(AssignParams p)
     const unsigned vmask = Co::template Pass<Plan<N>::NPASS - 1>::valid_mask(tid, p.m, p.F);
     double dsum = 0.0;
     int nchg = 0;
+    unsigned long long nev = 0;
     const int64_t stride = (int64_t)gridDim.x * TEAMS;
     for (int64_t i = (int64_t)blockIdx.x * TEAMS + team; i < p.n; i += stride) {
         if (p.fixed && p.gate && !p.gate[p.fixed[i]]) {  // uniform over the team
@@ -286,24 +294,8 @@ __global__ void __launch_bounds__(Cfg<N>::BLOCK, 1) k_assign_fft(AssignParams p)
         float xhN = 0.f;
         double nrm2;
         forward_row<N>(p.x + (size_t)i * p.m, p.m, buf, tid, team, p.twN, p.twF, scr, 1.0, xh, xhN, nrm2);
-        int c0 = 0, c1 = p.k;
-        if (p.fixed) {
-            c0 = p.fixed[i];
-            c1 = c0 + 1;
-        }
-        // screened: the candidates in ascending order (every centroid that can be the
-        // first minimum), so the first strict minimum below is the unscreened one
-        const int32_t* cl = nullptr;
-        int ncl = -1;
-        if (p.cand) {
-            cl = p.cand + (size_t)i * SCREEN_CAP;
-            ncl = screen_list_len(cl, p.ncand[i], p.k);
-        }
-        const int iters = ncl >= 0 ? ncl : c1 - c0;
-        float bestd = 1e10f;  // get_pos_idx: min_val = 1e10, pos = 0
-        int bestj = 0, bests = 0;
-        for (int it = 0; it < iters; ++it) {
-            const int c = ncl >= 0 ? cl[it] : c0 + it;
+        // max NCC of this series against centroid c (every thread of the team gets it)
+        auto eval = [&](int c) -> LagMax {
             float2 v[2][Co::R0];
             if (CSMEM) {
                 const float2* S = cspec + (size_t)c * (N + 1);
@@ -332,9 +324,67 @@ __global__ void __launch_bounds__(Cfg<N>::BLOCK, 1) k_assign_fft(AssignParams p)
                 lm = team_max<T>(lm, team, tid, scr);
             }
             team_sync<T>(team);
-            if (tid == 0) {
-                float d = 1.0f - lm.val;
-                if (p.clamp2 && d > 2.0f) d = 2.0f;
+            return lm;
+        };
+        auto distance = [&](const LagMax& lm) {
+            float d = 1.0f - lm.val;
+            if (p.clamp2 && d > 2.0f) d = 2.0f;
+            return d;
+        };
+        float bestd = 1e10f;  // get_pos_idx: min_val = 1e10, pos = 0
+        int bestj = 0, bests = 0;
+        if constexpr (BOUNDED) {
+            // the previous label first, then every other centroid in ascending order
+            // unless its bound (carried over with the centroid's movement) shows the
+            // distance exceeds the best so far: the same first minimum as evaluating all
+            // the label the previous assignment left in the output (read by every thread
+            // before thread 0 overwrites it, past the team barriers below)
+            int j0 = p.labels[i];
+            if (j0 < 0 || j0 >= p.k) j0 = p.old_labels ? p.old_labels[i] : 0;
+            if (j0 < 0 || j0 >= p.k) j0 = 0;
+            {
+                const float d = distance(eval(j0));
+                bestd = d;
+                bestj = j0;
+                if (tid == 0) p.lb_out[(size_t)j0 * p.n + i] = __fsub_rd(d, p.lb_eps);
+            }
+            int ne = 1;
+            for (int c = 0; c < p.k; ++c) {
+                if (c == j0) continue;
+                const float lb = __fsub_rd(__ldg(p.lb_in + (size_t)c * p.n + i), __ldg(p.delta + c));
+                if (__fsub_rd(lb, p.lb_eps) > bestd) {  // the same value in every thread: uniform
+                    if (tid == 0) p.lb_out[(size_t)c * p.n + i] = lb;
+                    continue;
+                }
+                const float d = distance(eval(c));
+                ++ne;
+                if (tid == 0) p.lb_out[(size_t)c * p.n + i] = __fsub_rd(d, p.lb_eps);
+                if (d < bestd || (d == bestd && c < bestj)) {
+                    bestd = d;
+                    bestj = c;
+                }
+            }
+            nev += (unsigned long long)ne;
+        } else {
+            int c0 = 0, c1 = p.k;
+            if (p.fixed) {
+                c0 = p.fixed[i];
+                c1 = c0 + 1;
+            }
+            // screened: the candidates in ascending order (every centroid that can be the
+            // first minimum), so the first strict minimum below is the unscreened one
+            const int32_t* cl = nullptr;
+            int ncl = -1;
+            if (p.cand) {
+                cl = p.cand + (size_t)i * SCREEN_CAP;
+                ncl = screen_list_len(cl, p.ncand[i], p.k);
+            }
+            const int iters = ncl >= 0 ? ncl : c1 - c0;
+            for (int it = 0; it < iters; ++it) {
+                const int c = ncl >= 0 ? cl[it] : c0 + it;
+                const LagMax lm = eval(c);
+                const float d = distance(lm);
+                if (tid == 0 && p.lb_out) p.lb_out[(size_t)c * p.n + i] = __fsub_rd(d, p.lb_eps);
                 if (d < bestd) {
                     bestd = d;
                     bestj = c;
@@ -353,6 +403,7 @@ __global__ void __launch_bounds__(Cfg<N>::BLOCK, 1) k_assign_fft(AssignParams p)
     if (tid == 0) {
         if (p.dist_sum) atomicAdd(p.dist_sum, dsum);
         if (p.changed && nchg) atomicAdd(p.changed, nchg);
+        if (BOUNDED && p.evals && nev) atomicAdd(p.evals, nev);
     }
 }
 
@@ -374,9 +425,9 @@ struct AssignPlan {
     int blocks_per_sm;  // 0: the occupancy maximum
 };
 
-template <int N, bool CSMEM, bool SHIFT>
+template <int N, bool CSMEM, bool SHIFT, bool BOUNDED>
 static void launch_variant(tc_ctx* ctx, const AssignParams& p, int blocks_per_sm, cudaStream_t s) {
-    auto fn = k_assign_fft<N, CSMEM, SHIFT>;
+    auto fn = k_assign_fft<N, CSMEM, SHIFT, BOUNDED>;
     allow_max_dynamic_smem(fn);
     const size_t sm = Cfg<N>::smem(p.k, CSMEM);
     int per_sm = 0;
@@ -388,10 +439,10 @@ static void launch_variant(tc_ctx* ctx, const AssignParams& p, int blocks_per_sm
     fn<<<grid, Cfg<N>::BLOCK, sm, s>>>(p);
 }
 
-template <int N, bool SHIFT>
+template <int N, bool SHIFT, bool BOUNDED>
 static void launch_plan(tc_ctx* ctx, const AssignParams& p, const AssignPlan& pl, cudaStream_t s) {
-    if (pl.csmem) launch_variant<N, true, SHIFT>(ctx, p, pl.blocks_per_sm, s);
-    else launch_variant<N, false, SHIFT>(ctx, p, pl.blocks_per_sm, s);
+    if (pl.csmem) launch_variant<N, true, SHIFT, BOUNDED>(ctx, p, pl.blocks_per_sm, s);
+    else launch_variant<N, false, SHIFT, BOUNDED>(ctx, p, pl.blocks_per_sm, s);
 }
 
 // Autotuner: the first assignment of a shape (FFT length, k, shift output) on a
@@ -401,11 +452,12 @@ static void launch_plan(tc_ctx* ctx, const AssignParams& p, const AssignPlan& pl
 // included.  Candidates: spectra in shared memory (when they fit) or not, times
 // the occupancy maximum, half of it and one block per SM.  Off with TIMESC_AUTOTUNE=0,
 // and never inside a stream capture (the default plan is used then).
-template <int N, bool SHIFT>
+template <int N, bool SHIFT, bool BOUNDED>
 static AssignPlan tuned_plan(tc_ctx* ctx, const AssignParams& p, cudaStream_t s) {
     const bool fits = Cfg<N>::smem(p.k, true) <= ctx->smem_optin;
     const AssignPlan dflt{fits, 0};
-    const uint64_t key = ((uint64_t)N << 40) | ((uint64_t)p.k << 8) | (SHIFT ? 1u : 0u) | (p.cand ? 2u : 0u);
+    const uint64_t key = ((uint64_t)N << 40) | ((uint64_t)p.k << 8) | (SHIFT ? 1u : 0u) | (p.cand ? 2u : 0u) |
+                         (BOUNDED ? 4u : 0u);
     for (const auto& t : ctx->tuned)
         if (t.first == key) return AssignPlan{(t.second & 1u) != 0, (int)(t.second >> 1)};
     const char* env = std::getenv("TIMESC_AUTOTUNE");
@@ -418,6 +470,7 @@ static AssignPlan tuned_plan(tc_ctx* ctx, const AssignParams& p, cudaStream_t s)
     q.n = sample;
     q.changed = nullptr;
     q.dist_sum = nullptr;
+    q.evals = nullptr;
     std::vector<AssignPlan> cands;
     for (int cs = fits ? 1 : 0; cs >= 0; --cs)
         for (int b : {0, -2, 1}) cands.push_back(AssignPlan{cs != 0, b});
@@ -430,17 +483,17 @@ static AssignPlan tuned_plan(tc_ctx* ctx, const AssignParams& p, cudaStream_t s)
         if (c.blocks_per_sm == -2) {  // half the occupancy maximum
             int per_sm = 0;
             if (c.csmem)
-                TC_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_assign_fft<N, true, SHIFT>,
-                                                                      Cfg<N>::BLOCK, Cfg<N>::smem(p.k, true)));
+                TC_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+                    &per_sm, k_assign_fft<N, true, SHIFT, BOUNDED>, Cfg<N>::BLOCK, Cfg<N>::smem(p.k, true)));
             else
-                TC_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_assign_fft<N, false, SHIFT>,
-                                                                      Cfg<N>::BLOCK, Cfg<N>::smem(p.k, false)));
+                TC_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+                    &per_sm, k_assign_fft<N, false, SHIFT, BOUNDED>, Cfg<N>::BLOCK, Cfg<N>::smem(p.k, false)));
             if (per_sm < 2) continue;
             c.blocks_per_sm = per_sm / 2;
         }
-        launch_plan<N, SHIFT>(ctx, q, c, s);  // warm
+        launch_plan<N, SHIFT, BOUNDED>(ctx, q, c, s);  // warm
         TC_CUDA(cudaEventRecord(e0, s));
-        for (int r = 0; r < 2; ++r) launch_plan<N, SHIFT>(ctx, q, c, s);
+        for (int r = 0; r < 2; ++r) launch_plan<N, SHIFT, BOUNDED>(ctx, q, c, s);
         TC_CUDA(cudaEventRecord(e1, s));
         TC_CUDA(cudaEventSynchronize(e1));
         TC_CUDA(cudaGetLastError());
@@ -455,15 +508,16 @@ static AssignPlan tuned_plan(tc_ctx* ctx, const AssignParams& p, cudaStream_t s)
     cudaEventDestroy(e1);
     ctx->tuned.emplace_back(key, (uint32_t)(pick.csmem ? 1 : 0) | ((uint32_t)pick.blocks_per_sm << 1));
     if (std::getenv("TIMESC_TRACE"))
-        std::fprintf(stderr, "timesc: autotune assignment F=%d k=%d shift=%d -> spectra %s, %d blocks/SM\n",
-                     2 * N, p.k, (int)SHIFT, pick.csmem ? "in shared memory" : "through L1", pick.blocks_per_sm);
+        std::fprintf(stderr, "timesc: autotune assignment F=%d k=%d shift=%d bounded=%d -> spectra %s, %d blocks/SM\n",
+                     2 * N, p.k, (int)SHIFT, (int)BOUNDED, pick.csmem ? "in shared memory" : "through L1",
+                     pick.blocks_per_sm);
     return pick;
 }
 
 template <int N>
 static void assign_n(tc_ctx* ctx, const AssignArgs& a, cudaStream_t s) {
     const FftTables& tb = fft_tables(ctx, 2 * N);
-    AssignParams p;
+    AssignParams p{};
     p.x = a.x;
     p.spec = a.spec;
     p.twN = (const float2*)tb.twN.p;
@@ -483,9 +537,87 @@ static void assign_n(tc_ctx* ctx, const AssignArgs& a, cudaStream_t s) {
     p.dist_sum = a.dist_sum;
     p.cand = a.cand;
     p.ncand = a.ncand;
+    p.lb_out = a.lb_out;
+    p.lb_in = a.lb_in;
+    p.delta = a.delta;
+    p.lb_eps = a.lb_eps;
+    p.evals = a.evals;
     const bool want_shift = a.shift != nullptr || a.fixed != nullptr;
-    if (want_shift) launch_plan<N, true>(ctx, p, tuned_plan<N, true>(ctx, p, s), s);
-    else launch_plan<N, false>(ctx, p, tuned_plan<N, false>(ctx, p, s), s);
+    if (a.lb_in) {
+        // the bounded pass exists where its bounds come from: the screened lengths (F 128..1024)
+        if constexpr (N >= 64 && N <= 512) {
+            TC_REQUIRE(!want_shift && a.lb_out && a.delta, TC_ERR_ARG, "bounded assignment: arguments");
+            launch_plan<N, false, true>(ctx, p, tuned_plan<N, false, true>(ctx, p, s), s);
+        } else {
+            throw TcError{TC_ERR_UNSUPPORTED, "bounded assignment: FFT length outside 128..1024"};
+        }
+    } else if (want_shift) {
+        launch_plan<N, true, false>(ctx, p, tuned_plan<N, true, false>(ctx, p, s), s);
+    } else {
+        launch_plan<N, false, false>(ctx, p, tuned_plan<N, false, false>(ctx, p, s), s);
+    }
+    TC_CHECK_LAUNCH();
+}
+
+// ------------------------------------------------------------------ centroid movement
+// delta[j] >= |c_j/|c_j| - cprev_j| (FP64 sums, rounded up with a margin for the FP32
+// storage of cprev), +inf where exactly one of the two is zero; then cprev_j <- the
+// unit centroid (zeros for a zero centroid).  The NCC of a series with c_j moves by
+// at most delta[j] at every lag (the lags are norm-preserving or norm-reducing
+// shifts of the unit centroid, Cauchy-Schwarz), and so does its distance.
+__global__ void __launch_bounds__(256) k_centroid_delta(const float* __restrict__ C, int m, float* __restrict__ cprev,
+                                                        float* __restrict__ delta) {
+    __shared__ double red[8][2];
+    __shared__ double sh[2];
+    const int j = blockIdx.x, lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    const float* c = C + (size_t)j * m;
+    float* cp = cprev + (size_t)j * m;
+    double a = 0, b = 0;
+    for (int t = threadIdx.x; t < m; t += 256) {
+        a += (double)c[t] * c[t];
+        b += (double)cp[t] * cp[t];
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        a += __shfl_xor_sync(0xffffffffu, a, o);
+        b += __shfl_xor_sync(0xffffffffu, b, o);
+    }
+    if (lane == 0) { red[wid][0] = a; red[wid][1] = b; }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double sa = 0, sb = 0;
+        for (int w = 0; w < 8; ++w) { sa += red[w][0]; sb += red[w][1]; }
+        sh[0] = sqrt(sa);
+        sh[1] = sqrt(sb);
+    }
+    __syncthreads();
+    const double nc = sh[0], np = sh[1];
+    double dd = 0;
+    if (nc > 0 && np > 0)
+        for (int t = threadIdx.x; t < m; t += 256) {
+            const double e = (double)c[t] / nc - (double)cp[t] / np;
+            dd += e * e;
+        }
+    for (int o = 16; o > 0; o >>= 1) dd += __shfl_xor_sync(0xffffffffu, dd, o);
+    __syncthreads();
+    if (lane == 0) red[wid][0] = dd;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        float dl;
+        if (nc > 0 && np > 0) {
+            double s2 = 0;
+            for (int w = 0; w < 8; ++w) s2 += red[w][0];
+            dl = __double2float_ru(sqrt(s2) * (1.0 + 1e-6) + 1e-6);
+        } else {
+            dl = (nc > 0) != (np > 0) ? __int_as_float(0x7f800000) : 0.f;  // +inf / unchanged zero
+        }
+        delta[j] = dl;
+    }
+    __syncthreads();  // every read of cprev is done
+    for (int t = threadIdx.x; t < m; t += 256) cp[t] = nc > 0 ? (float)((double)c[t] / nc) : 0.f;
+}
+
+void launch_centroid_delta(const float* C, int k, int m, float* cprev, float* delta, cudaStream_t s) {
+    k_centroid_delta<<<k, 256, 0, s>>>(C, m, cprev, delta);
     TC_CHECK_LAUNCH();
 }
 
@@ -596,7 +728,7 @@ static void noalloc_n(const NoallocDevice& d, const float* x, const float* C, in
     p.dist = dist;
     const bool csmem = Cfg<N>::smem(k, true) <= d.smem_optin;
     const size_t sm = Cfg<N>::smem(k, csmem);
-    auto fn = csmem ? k_assign_fft<N, true, false> : k_assign_fft<N, false, false>;
+    auto fn = csmem ? k_assign_fft<N, true, false, false> : k_assign_fft<N, false, false, false>;
     allow_max_dynamic_smem(fn);
     int per_sm = 0;
     TC_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, Cfg<N>::BLOCK, sm));

@@ -162,6 +162,9 @@ struct AtParams {
     int32_t* cand;
     int32_t* ncand;
     float thr;
+    // lower bounds d - lb_d16 on the exact distance of every pair, [k][n] (or null)
+    float* lb_out;
+    float lb_d16;
 };
 
 // Keep the list entries with distance <= lim (NaN kept), in order; returns the count.
@@ -364,6 +367,7 @@ __global__ void __launch_bounds__(AT_THREADS, 1) k_assign_tc(const __grid_consta
                 const float ncc = den > 0.f ? mx / den : 0.f;  // a zero norm gives NCC 0 (ncc.cuh:89)
                 float d = 1.0f - ncc;
                 if (p.clamp2 && d > 2.0f) d = 2.0f;
+                if (p.lb_out && i < p.n) p.lb_out[(size_t)j * p.n + i] = __fsub_rd(d, p.lb_d16);
                 if (d < bestd) {
                     bestd = d;
                     bestj = j;
@@ -440,6 +444,7 @@ void prepare_series_bf16_done(tc_ctx* ctx, const float* x, int64_t n, int m) {
     ctx->prep_x = x;
     ctx->prep_n = n;
     ctx->prep_m = m;
+    ctx->bounds.valid = false;  // new series contents: bounds on old distances no longer hold
 }
 
 void prepare_series_bf16(tc_ctx* ctx, const float* x, int64_t n, int m, cudaStream_t s) {
@@ -477,17 +482,19 @@ bool screen_supported(int m, int F, int k) {
 // 2-norm after the 1/F-scaled inverse, whose own error adds L eta |r|_2 <= L eta sqrt(m)
 // (|r|_2 <= |x|_1 |c|_2 <= sqrt(m), Young).  A lag's error is at most the 2-norm; the
 // bound is doubled for the normalisation's few roundings and the O(L eta) terms.
-static double fft_error(int m, int F) {
+double fft_error(int m, int F) {
     const double u = std::ldexp(1.0, -24), g4 = 4 * u / (1 - 4 * u);
     const double eta = u + g4 * (std::sqrt(2.0) + u);
     const double L = std::log2((double)F);
     return 2.0 * (3.0 * L * eta + 3.0 * u) * std::sqrt((double)m);
 }
 
-static float screen_threshold(int mp, int m, int F) {
-    const double D = std::ldexp(1.0, -8) + std::ldexp(1.0, -18) + mp * std::ldexp(1.0, -21) + fft_error(m, F);
-    return (float)(2.0 * D * (1.0 + 1e-3));
+double bf16_error(int m, int F) {
+    const int mp = (m + 63) / 64 * 64;
+    return std::ldexp(1.0, -8) + std::ldexp(1.0, -18) + mp * std::ldexp(1.0, -21) + fft_error(m, F);
 }
+
+static float screen_threshold(int m, int F) { return (float)(2.0 * bf16_error(m, F) * (1.0 + 1e-3)); }
 
 void launch_assign_tc(tc_ctx* ctx, const AssignArgs& a, int precision, cudaStream_t s) {
     TC_REQUIRE(tc_assign_supported(a.m, a.F, a.k, precision), TC_ERR_UNSUPPORTED, "tensor-core correlation shape");
@@ -526,7 +533,9 @@ void launch_assign_tc(tc_ctx* ctx, const AssignArgs& a, int precision, cudaStrea
     if (a.cand) {
         p.cand = a.cand;
         p.ncand = a.ncand;
-        p.thr = screen_threshold(g.mp, a.m, a.F);
+        p.lb_out = a.lb_out;
+        p.lb_d16 = a.lb_d16;
+        p.thr = screen_threshold(a.m, a.F);
         p.labels = nullptr;
         p.dist = nullptr;
         p.old_labels = nullptr;

@@ -140,6 +140,20 @@ struct Workspace {
     DevBuf xbf;          // bf16 copy of the series for the tensor-core correlation
     DevBuf xbf_norm;     // n f32 series norms
     DevBuf screen;       // n x SCREEN_CAP candidate centroids + n counts (screened FP32 assignment)
+    DevBuf bounds;       // 2 x k x n f32: lower bounds in / out (bounded assignment)
+    DevBuf cprev;        // k x m f32 unit centroids the bounds refer to, + k f32 movements
+};
+
+// State of the bounded assignment across iterations: the bounds in ws.bounds are
+// valid for these series and the unit centroids in ws.cprev.
+struct BoundsState {
+    const float* x = nullptr;
+    int64_t n = 0;
+    int m = 0, k = 0, mode = -1;
+    bool valid = false;
+    bool refresh = true;  // next assignment: the screened pass (new bounds)
+    // totals for tc_assign_stats
+    uint64_t screened = 0, bounded = 0, bounded_pairs = 0;
 };
 
 struct tc_ctx {
@@ -159,6 +173,8 @@ struct tc_ctx {
     const float* prep_x = nullptr;
     int64_t prep_n = 0;
     int prep_m = 0;
+    // bounded assignment (used for prepared series and inside tc_kshape_run)
+    BoundsState bounds;
 };
 
 namespace tc {
@@ -192,8 +208,29 @@ struct AssignArgs {
     // FFT pass evaluates only those
     int32_t* cand;
     int32_t* ncand;
+    // lower bounds on the exact distance of every (series, centroid) pair, centroid-major
+    // [k][n] (the bounded assignment across iterations; see assign_fft.cu):
+    //   lb_out  written: the tensor-core pass d16 - lb_d16 for every pair, the FFT passes
+    //           d32 - lb_eps for every pair they evaluate, the bounded pass also the
+    //           carried bounds of the pairs it skips
+    //   lb_in   read by the bounded pass (bounds for the previous centroids), with
+    //           delta[j] >= |c_j/|c_j| - c'_j/|c'_j|| the movement of centroid j
+    float* lb_out;
+    const float* lb_in;
+    const float* delta;
+    float lb_eps;   // bound on |d32 - d| of the FFT kernel (fft_error)
+    float lb_d16;   // bound on |d16 - d| of the tensor-core pass
+    unsigned long long* evals;  // bounded pass: pairs evaluated (accumulated)
 };
 void launch_assign_fft(tc_ctx* ctx, const AssignArgs& a, cudaStream_t s);
+// movement of every centroid since cprev (unit vectors, k x m), then cprev <- the unit
+// centroids; delta[j] is rounded up, and +inf where one of the two is zero and the
+// other not
+void launch_centroid_delta(const float* C, int k, int m, float* cprev, float* delta, cudaStream_t s);
+// worst-case |d32 - d| of the FP32 FFT correlation for unit-norm series and centroids
+double fft_error(int m, int F);
+// worst-case |d16 - d32| of the BF16 tensor-core correlation (the screen's half-width)
+double bf16_error(int m, int F);
 
 // tensor-core correlation (tcgen05); returns false when the shape is not supported
 bool tc_assign_supported(int m, int F, int k, int precision);

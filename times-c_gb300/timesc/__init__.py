@@ -62,6 +62,8 @@ SIGNATURES = {
     "tc_init_labels": (_int, [_vp, _vp, _i64, _int, _vp]),
     "tc_sbd_assign": (_int, [_vp, _vp, _vp, _i64, _int, _int, _int, _int, _vp, _vp, _vp, _vp, _vp, _vp, _vp]),
     "tc_prepare_series": (_int, [_vp, _vp, _i64, _int, _vp]),
+    "tc_assign_stats": (_int, [_vp, ctypes.POINTER(ctypes.c_uint64), ctypes.POINTER(ctypes.c_uint64),
+                               ctypes.POINTER(ctypes.c_uint64)]),
     "tc_sbd_assign_noalloc": (_int, [_vp, _vp, _i64, _int, _int, _int, _vp, _vp, _vp, ctypes.c_char_p, _int]),
     "tc_extract_shapes": (_int, [_vp, _vp, _vp, _vp, _vp, _i64, _int, _int, _int, _int, _int, _vp,
                                  ctypes.POINTER(_int), _vp]),
@@ -164,6 +166,13 @@ class Context:
         self._check(lib().tc_sbd_assign(self.h, _ptr(x), _ptr(C), n, m, k, mode, precision, _ptr(labels),
                                         _ptr(dist), _ptr(shift), _ptr(old_labels), _ptr(changed),
                                         _ptr(dist_sum), _stream(stream)))
+
+    def assign_stats(self):
+        """(screened, bounded, bounded_pairs): FP32 assignments that built distance bounds,
+        that used them, and the (series, centroid) pairs the bounded ones evaluated."""
+        a, b, c = ctypes.c_uint64(), ctypes.c_uint64(), ctypes.c_uint64()
+        self._check(lib().tc_assign_stats(self.h, ctypes.byref(a), ctypes.byref(b), ctypes.byref(c)))
+        return a.value, b.value, c.value
 
     def prepare_series(self, x, stream=None):
         """Keep a BF16 copy of x for TC_PREC_BF16 assignments on the same tensor."""
