@@ -102,7 +102,7 @@ static int assign(tc_ctx* ctx, const float* x, const float* C, int64_t n, int m,
         float *lb = nullptr, *delta = nullptr;
         unsigned long long* evals = reinterpret_cast<unsigned long long*>(ws.aux.as<char>(64) + 24);
         if (use != BOUNDS_OFF) {
-            lb = ws.bounds.as<float>((size_t)2 * k * n);
+            lb = ws.bounds.as<float>((size_t)k * n);
             float* cprev = ws.cprev.as<float>((size_t)k * m + k);
             delta = cprev + (size_t)k * m;
             launch_centroid_delta(C, k, m, cprev, delta, s);  // cprev <- these centroids
@@ -114,11 +114,10 @@ static int assign(tc_ctx* ctx, const float* x, const float* C, int64_t n, int m,
         a.spec = spec;
         if (use == BOUNDS_USE) {
             a.lb_in = lb;
-            a.lb_out = lb + (size_t)k * n;
+            a.lb_out = lb;  // updated in place
             a.delta = delta;
             a.evals = evals;
             launch_assign_fft(ctx, a, s);
-            TC_CUDA(cudaMemcpyAsync(lb, lb + (size_t)k * n, sizeof(float) * k * n, cudaMemcpyDeviceToDevice, s));
             return use;
         }
         // exact screening: the BF16 pass keeps every centroid whose FP32 distance can be

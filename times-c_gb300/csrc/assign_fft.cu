@@ -178,9 +178,11 @@ struct Cfg {
     static constexpr int BLOCK = T > 512 ? T : 512;
     static constexpr int TEAMS = BLOCK / T;
     static constexpr size_t BUF_BYTES = (size_t)BufSize<N>::value * sizeof(float2);
-    static size_t smem(int k, bool csmem) {
+    static constexpr int LBC = 32;  // bounded pass: bounds staged per team, a chunk of centroids at a time
+    static size_t smem(int k, bool csmem, bool bounded = false) {
         size_t s = (size_t)TEAMS * (BUF_BYTES + sizeof(TeamScratch));
         if (csmem) s += ((size_t)k * (N + 1) * sizeof(float2) + 15) / 16 * 16;  // as laid out in the kernel
+        if (bounded) s += (size_t)TEAMS * 2 * LBC * sizeof(float);
         return s;
     }
 };
@@ -273,6 +275,8 @@ __global__ void __launch_bounds__(Cfg<N>::BLOCK, 1) k_assign_fft(AssignParams p)
     const int team = threadIdx.x / T, tid = threadIdx.x % T;
     float2* buf = reinterpret_cast<float2*>(cur) + (size_t)team * BufSize<N>::value;
     TeamScratch* scr = reinterpret_cast<TeamScratch*>(cur + (size_t)TEAMS * Cfg<N>::BUF_BYTES) + team;
+    float* lbs = reinterpret_cast<float*>(cur + (size_t)TEAMS * (Cfg<N>::BUF_BYTES + sizeof(TeamScratch))) +
+                 (size_t)team * 2 * Cfg<N>::LBC;  // bounded pass: this team's bounds in, then out
 
     if (CSMEM) {
         const size_t nv = (size_t)p.k * (N + 1);
@@ -336,33 +340,49 @@ __global__ void __launch_bounds__(Cfg<N>::BLOCK, 1) k_assign_fft(AssignParams p)
         if constexpr (BOUNDED) {
             // the previous label first, then every other centroid in ascending order
             // unless its bound (carried over with the centroid's movement) shows the
-            // distance exceeds the best so far: the same first minimum as evaluating all
+            // distance exceeds the best so far: the same first minimum as evaluating all.
+            // The bounds (series-major, p.lb_in == p.lb_out allowed) are staged through
+            // shared memory LBC centroids at a time: a chunk is read by the whole team
+            // into lbs, decided on (new bounds into a second array), and written back
+            // after a team barrier, so no thread reads a bound another has rewritten.
             // the label the previous assignment left in the output (read by every thread
             // before thread 0 overwrites it, past the team barriers below)
             int j0 = p.labels[i];
             if (j0 < 0 || j0 >= p.k) j0 = p.old_labels ? p.old_labels[i] : 0;
             if (j0 < 0 || j0 >= p.k) j0 = 0;
-            {
-                const float d = distance(eval(j0));
-                bestd = d;
-                bestj = j0;
-                if (tid == 0) p.lb_out[(size_t)j0 * p.n + i] = __fsub_rd(d, p.lb_eps);
-            }
+            const float d0 = distance(eval(j0));
+            bestd = d0;
+            bestj = j0;
             int ne = 1;
-            for (int c = 0; c < p.k; ++c) {
-                if (c == j0) continue;
-                const float lb = __fsub_rd(__ldg(p.lb_in + (size_t)c * p.n + i), __ldg(p.delta + c));
-                if (__fsub_rd(lb, p.lb_eps) > bestd) {  // the same value in every thread: uniform
-                    if (tid == 0) p.lb_out[(size_t)c * p.n + i] = lb;
-                    continue;
+            const float* lbi = p.lb_in + (size_t)i * p.k;
+            float* lbo = p.lb_out + (size_t)i * p.k;
+            constexpr int LBC = Cfg<N>::LBC;
+            for (int c0 = 0; c0 < p.k; c0 += LBC) {
+                const int nc = min(LBC, p.k - c0);
+                for (int t = tid; t < nc; t += T) lbs[t] = __fsub_rd(__ldg(lbi + c0 + t), __ldg(p.delta + c0 + t));
+                team_sync<T>(team);
+                for (int t = 0; t < nc; ++t) {
+                    const int c = c0 + t;
+                    const float lb = lbs[t];  // the same value in every thread: decisions are uniform
+                    float nb;
+                    if (c == j0) {
+                        nb = __fsub_rd(d0, p.lb_eps);
+                    } else if (__fsub_rd(lb, p.lb_eps) > bestd) {
+                        nb = lb;
+                    } else {
+                        const float d = distance(eval(c));  // ends with a team barrier
+                        ++ne;
+                        nb = __fsub_rd(d, p.lb_eps);
+                        if (d < bestd || (d == bestd && c < bestj)) {
+                            bestd = d;
+                            bestj = c;
+                        }
+                    }
+                    if (tid == 0) lbs[LBC + t] = nb;
                 }
-                const float d = distance(eval(c));
-                ++ne;
-                if (tid == 0) p.lb_out[(size_t)c * p.n + i] = __fsub_rd(d, p.lb_eps);
-                if (d < bestd || (d == bestd && c < bestj)) {
-                    bestd = d;
-                    bestj = c;
-                }
+                team_sync<T>(team);
+                for (int t = tid; t < nc; t += T) lbo[c0 + t] = lbs[LBC + t];
+                team_sync<T>(team);  // the next chunk overwrites lbs
             }
             nev += (unsigned long long)ne;
         } else {
@@ -384,7 +404,7 @@ __global__ void __launch_bounds__(Cfg<N>::BLOCK, 1) k_assign_fft(AssignParams p)
                 const int c = ncl >= 0 ? cl[it] : c0 + it;
                 const LagMax lm = eval(c);
                 const float d = distance(lm);
-                if (tid == 0 && p.lb_out) p.lb_out[(size_t)c * p.n + i] = __fsub_rd(d, p.lb_eps);
+                if (tid == 0 && p.lb_out) p.lb_out[(size_t)i * p.k + c] = __fsub_rd(d, p.lb_eps);
                 if (d < bestd) {
                     bestd = d;
                     bestj = c;
@@ -429,7 +449,7 @@ template <int N, bool CSMEM, bool SHIFT, bool BOUNDED>
 static void launch_variant(tc_ctx* ctx, const AssignParams& p, int blocks_per_sm, cudaStream_t s) {
     auto fn = k_assign_fft<N, CSMEM, SHIFT, BOUNDED>;
     allow_max_dynamic_smem(fn);
-    const size_t sm = Cfg<N>::smem(p.k, CSMEM);
+    const size_t sm = Cfg<N>::smem(p.k, CSMEM, BOUNDED);
     int per_sm = 0;
     TC_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, Cfg<N>::BLOCK, sm));
     per_sm = std::max(per_sm, 1);
@@ -454,7 +474,7 @@ static void launch_plan(tc_ctx* ctx, const AssignParams& p, const AssignPlan& pl
 // and never inside a stream capture (the default plan is used then).
 template <int N, bool SHIFT, bool BOUNDED>
 static AssignPlan tuned_plan(tc_ctx* ctx, const AssignParams& p, cudaStream_t s) {
-    const bool fits = Cfg<N>::smem(p.k, true) <= ctx->smem_optin;
+    const bool fits = Cfg<N>::smem(p.k, true, BOUNDED) <= ctx->smem_optin;
     const AssignPlan dflt{fits, 0};
     const uint64_t key = ((uint64_t)N << 40) | ((uint64_t)p.k << 8) | (SHIFT ? 1u : 0u) | (p.cand ? 2u : 0u) |
                          (BOUNDED ? 4u : 0u);
@@ -484,10 +504,12 @@ static AssignPlan tuned_plan(tc_ctx* ctx, const AssignParams& p, cudaStream_t s)
             int per_sm = 0;
             if (c.csmem)
                 TC_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-                    &per_sm, k_assign_fft<N, true, SHIFT, BOUNDED>, Cfg<N>::BLOCK, Cfg<N>::smem(p.k, true)));
+                    &per_sm, k_assign_fft<N, true, SHIFT, BOUNDED>, Cfg<N>::BLOCK,
+                    Cfg<N>::smem(p.k, true, BOUNDED)));
             else
                 TC_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-                    &per_sm, k_assign_fft<N, false, SHIFT, BOUNDED>, Cfg<N>::BLOCK, Cfg<N>::smem(p.k, false)));
+                    &per_sm, k_assign_fft<N, false, SHIFT, BOUNDED>, Cfg<N>::BLOCK,
+                    Cfg<N>::smem(p.k, false, BOUNDED)));
             if (per_sm < 2) continue;
             c.blocks_per_sm = per_sm / 2;
         }

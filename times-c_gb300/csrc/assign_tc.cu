@@ -162,7 +162,7 @@ struct AtParams {
     int32_t* cand;
     int32_t* ncand;
     float thr;
-    // lower bounds d - lb_d16 on the exact distance of every pair, [k][n] (or null)
+    // lower bounds d - lb_d16 on the exact distance of every pair, [n][k] (or null)
     float* lb_out;
     float lb_d16;
 };
@@ -367,7 +367,7 @@ __global__ void __launch_bounds__(AT_THREADS, 1) k_assign_tc(const __grid_consta
                 const float ncc = den > 0.f ? mx / den : 0.f;  // a zero norm gives NCC 0 (ncc.cuh:89)
                 float d = 1.0f - ncc;
                 if (p.clamp2 && d > 2.0f) d = 2.0f;
-                if (p.lb_out && i < p.n) p.lb_out[(size_t)j * p.n + i] = __fsub_rd(d, p.lb_d16);
+                if (p.lb_out && i < p.n) p.lb_out[(size_t)i * p.k + j] = __fsub_rd(d, p.lb_d16);
                 if (d < bestd) {
                     bestd = d;
                     bestj = j;

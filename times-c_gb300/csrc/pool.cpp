@@ -203,7 +203,7 @@ uint64_t tc_job_footprint(const tc_job* j) {
         b += n * mp * 2 + n * 4;           // BF16 series and norms
         b += k * (F / 8) * (mp + 56) * 2 + k * 4;  // shifted centroid buffers
     }
-    if (screened) b += n * (tc::SCREEN_CAP + 1) * 4 + 2 * k * n * 4 + (k * m + k) * 4;  // candidates, bounds
+    if (screened) b += n * (tc::SCREEN_CAP + 1) * 4 + k * n * 4 + (k * m + k) * 4;  // candidates, bounds
     b += ((n + 4095) / 4096) * k * 4;      // segment chunk counts
     return b + (1u << 20);
 }

@@ -140,7 +140,7 @@ struct Workspace {
     DevBuf xbf;          // bf16 copy of the series for the tensor-core correlation
     DevBuf xbf_norm;     // n f32 series norms
     DevBuf screen;       // n x SCREEN_CAP candidate centroids + n counts (screened FP32 assignment)
-    DevBuf bounds;       // 2 x k x n f32: lower bounds in / out (bounded assignment)
+    DevBuf bounds;       // n x k f32: distance lower bounds (bounded assignment)
     DevBuf cprev;        // k x m f32 unit centroids the bounds refer to, + k f32 movements
 };
 
@@ -208,13 +208,14 @@ struct AssignArgs {
     // FFT pass evaluates only those
     int32_t* cand;
     int32_t* ncand;
-    // lower bounds on the exact distance of every (series, centroid) pair, centroid-major
-    // [k][n] (the bounded assignment across iterations; see assign_fft.cu):
+    // lower bounds on the exact distance of every (series, centroid) pair, series-major
+    // [n][k] (the bounded assignment across iterations; see assign_fft.cu):
     //   lb_out  written: the tensor-core pass d16 - lb_d16 for every pair, the FFT passes
     //           d32 - lb_eps for every pair they evaluate, the bounded pass also the
     //           carried bounds of the pairs it skips
     //   lb_in   read by the bounded pass (bounds for the previous centroids), with
-    //           delta[j] >= |c_j/|c_j| - c'_j/|c'_j|| the movement of centroid j
+    //           delta[j] >= |c_j/|c_j| - c'_j/|c'_j|| the movement of centroid j; it may
+    //           be lb_out (updated in place)
     float* lb_out;
     const float* lb_in;
     const float* delta;
