@@ -1,13 +1,13 @@
-"""The FP32 assignment with distance bounds carried across iterations gives
-exactly the labels, distances and centroids of evaluating every pair.
+"""Assignments with distance bounds carried across iterations give exactly the
+labels, distances and centroids of evaluating every pair.
 
 On series kept fixed across calls (tc_prepare_series, and inside tc_kshape_run)
-a screened FP32 assignment leaves a lower bound on every (series, centroid)
-distance; the next assignments lower each bound by its centroid's movement and
-evaluate only pairs whose bound does not exceed the series' best distance so far
-(previous label first).  TIMESC_NO_BOUNDS=1 turns that off: both runs must agree
-bit for bit, on ordinary data, exact ties, a zero centroid and a centroid that
-flips sign.
+a full assignment leaves a lower bound on every (series, centroid) distance; the
+next assignments lower each bound by its centroid's movement and evaluate only
+the pairs the bounds do not rule out - per series in the FP32 form (previous
+label first), per 128-row tile of series grouped by their best centroid in the
+BF16 form.  TIMESC_NO_BOUNDS=1 turns that off: both runs must agree bit for bit,
+on ordinary data, exact ties, a zero centroid and a centroid that flips sign.
 """
 import os
 
@@ -17,17 +17,18 @@ import pytest
 pytestmark = pytest.mark.gpu
 
 
-def _run(ctx, data, k, mode, init_chose, seed, bounds, cap=30):
+def _run(ctx, data, k, mode, init_chose, seed, bounds, prec=0, cap=30):
     if bounds:
         os.environ.pop("TIMESC_NO_BOUNDS", None)
     else:
         os.environ["TIMESC_NO_BOUNDS"] = "1"
     try:
-        return ctx.kshape_run(data, k, mode=mode, precision=0, init_chose=init_chose, seed=seed, max_iter=cap)
+        return ctx.kshape_run(data, k, mode=mode, precision=prec, init_chose=init_chose, seed=seed, max_iter=cap)
     finally:
         os.environ.pop("TIMESC_NO_BOUNDS", None)
 
 
+@pytest.mark.parametrize("prec", [0, 1])
 @pytest.mark.parametrize("mode,n,m,k,init_chose", [
     (0, 3000, 128, 4, 0),      # compat, F = 128
     (0, 2000, 100, 5, 0),      # compat pad-with-2 (2m - 1 < 512)
@@ -35,20 +36,20 @@ def _run(ctx, data, k, mode, init_chose, seed, bounds, cap=30):
     (1, 3000, 200, 6, 0),      # canonical, F = 512
     (0, 8000, 512, 32, 0),     # the precision configuration's shape, smaller n
 ])
-def test_loop_with_bounds_equals_dense(built, mode, n, m, k, init_chose):
+def test_loop_with_bounds_equals_dense(built, prec, mode, n, m, k, init_chose):
     T, _ = built
     data, _ = T.generate(n, m, k, noise=0.3, seed=n + m)
     ctx = T.Context(0)
     try:
         s0 = ctx.assign_stats()
-        a = _run(ctx, data, k, mode, init_chose, 3, bounds=True)
+        a = _run(ctx, data, k, mode, init_chose, 3, bounds=True, prec=prec)
         s1 = ctx.assign_stats()
-        b = _run(ctx, data, k, mode, init_chose, 3, bounds=False)
+        b = _run(ctx, data, k, mode, init_chose, 3, bounds=False, prec=prec)
     finally:
         ctx.close()
     bounded, pairs = s1[1] - s0[1], s1[2] - s0[2]
-    print("n=%d m=%d k=%d mode=%d: %d iterations, %d bounded passes, %.3f of their pairs evaluated"
-          % (n, m, k, mode, a["iterations"], bounded, pairs / max(1, bounded * n * k)))
+    print("prec=%d n=%d m=%d k=%d mode=%d: %d iterations, %d bounded passes, %.3f of their pairs evaluated"
+          % (prec, n, m, k, mode, a["iterations"], bounded, pairs / max(1, bounded * n * k)))
     assert a["iterations"] == b["iterations"]
     assert a["sum_class"] == b["sum_class"] and a["restarted"] == b["restarted"]
     assert np.array_equal(a["labels"], b["labels"])
@@ -57,7 +58,8 @@ def test_loop_with_bounds_equals_dense(built, mode, n, m, k, init_chose):
         assert bounded >= 1
 
 
-def test_stage_calls_with_bounds_ties_zero_and_flip(built):
+@pytest.mark.parametrize("prec", [0, 1])
+def test_stage_calls_with_bounds_ties_zero_and_flip(built, prec):
     """Stage calls on prepared series: each call with bounds against a context that
     evaluates every pair, over a sequence of centroid sets with small moves, an exact
     duplicate (ties go to the first index even when the previous label is the later
@@ -96,10 +98,10 @@ def test_stage_calls_with_bounds_ties_zero_and_flip(built):
                 lab_b.fill_(5)  # previous label the later duplicate: the first index must still win
             db = torch.zeros(n, dtype=torch.float32, device="cuda")
             dd = torch.zeros(n, dtype=torch.float32, device="cuda")
-            ctx_b.sbd_assign(x, cg, mode=0, precision=0, labels=lab_b, dist=db)
+            ctx_b.sbd_assign(x, cg, mode=0, precision=prec, labels=lab_b, dist=db)
             os.environ["TIMESC_NO_BOUNDS"] = "1"
             try:
-                ctx_d.sbd_assign(x, cg, mode=0, precision=0, labels=lab_d, dist=dd)
+                ctx_d.sbd_assign(x, cg, mode=0, precision=prec, labels=lab_d, dist=dd)
             finally:
                 os.environ.pop("TIMESC_NO_BOUNDS", None)
             torch.cuda.synchronize()
@@ -111,6 +113,6 @@ def test_stage_calls_with_bounds_ties_zero_and_flip(built):
     finally:
         ctx_b.close()
         ctx_d.close()
-    print("stage sequence: %d screened, %d bounded, %d pairs evaluated by the bounded calls"
-          % (s1[0] - s0[0], s1[1] - s0[1], s1[2] - s0[2]))
+    print("prec=%d stage sequence: %d full, %d bounded, %d pairs evaluated by the bounded calls"
+          % (prec, s1[0] - s0[0], s1[1] - s0[1], s1[2] - s0[2]))
     assert s1[1] - s0[1] >= 3

@@ -61,9 +61,32 @@ static void check_shape(int64_t n, int m, int k, int mode) {
 enum { BOUNDS_OFF = 0, BOUNDS_AUTO = -1, BOUNDS_REFRESH = 1, BOUNDS_USE = 2 };
 constexpr double BOUNDS_REFRESH_FRACTION = 0.3;
 
+// Bounds are kept for the FP32 form where the screened pass runs, and for the BF16
+// form where the tensor-core correlation runs with k <= 64 (one mask word per tile).
 static bool bounds_usable(const tc_ctx* ctx, const float* x, int64_t n, int m, int k, int mode, int precision) {
-    return precision == TC_PREC_FP32 && screen_supported(m, fft_size(m, mode), k) && !std::getenv("TIMESC_NO_BOUNDS") &&
-           ctx->prep_x == x && ctx->prep_n == n && ctx->prep_m == m;
+    const int F = fft_size(m, mode);
+    const bool form = precision == TC_PREC_FP32 ? screen_supported(m, F, k)
+                                                : (tc_assign_supported(m, F, k, precision) && k >= 2 && k <= 64);
+    return form && !std::getenv("TIMESC_NO_BOUNDS") && ctx->prep_x == x && ctx->prep_n == n && ctx->prep_m == m;
+}
+
+// The bounds state for these series and shape (reset when any of them changes).
+static BoundsState& bounds_for(tc_ctx* ctx, const float* x, int64_t n, int m, int k, int mode, int precision) {
+    BoundsState& b = ctx->bounds;
+    if (!(b.x == x && b.n == n && b.m == m && b.k == k && b.mode == mode && b.precision == precision)) {
+        const uint64_t sc = b.screened, bd = b.bounded, bp = b.bounded_pairs;
+        b = BoundsState{};
+        b.x = x;
+        b.n = n;
+        b.m = m;
+        b.k = k;
+        b.mode = mode;
+        b.precision = precision;
+        b.screened = sc;
+        b.bounded = bd;
+        b.bounded_pairs = bp;
+    }
+    return b;
 }
 
 // One assignment against the current centroids.  Returns the bounds mode it ran.
@@ -86,16 +109,8 @@ static int assign(tc_ctx* ctx, const float* x, const float* C, int64_t n, int m,
     a.dist_sum = dsum;
     if (precision == TC_PREC_FP32 && !shift && screen_supported(m, F, k)) {
         Workspace& ws = ctx->ws;
-        BoundsState& b = ctx->bounds;
         const bool usable = bmode != BOUNDS_OFF && bounds_usable(ctx, x, n, m, k, mode, precision);
-        if (usable && !(b.x == x && b.n == n && b.m == m && b.k == k && b.mode == mode)) {
-            b = BoundsState{};
-            b.x = x;
-            b.n = n;
-            b.m = m;
-            b.k = k;
-            b.mode = mode;
-        }
+        BoundsState& b = usable ? bounds_for(ctx, x, n, m, k, mode, precision) : ctx->bounds;
         int use = BOUNDS_OFF;
         if (usable) use = bmode == BOUNDS_AUTO ? (b.valid && !b.refresh ? BOUNDS_USE : BOUNDS_REFRESH) : bmode;
         if (use == BOUNDS_USE && !b.valid) use = BOUNDS_REFRESH;
@@ -146,11 +161,49 @@ static int assign(tc_ctx* ctx, const float* x, const float* C, int64_t n, int m,
         launch_centroid_spectra(ctx, C, k, m, F, spec, s);
         a.spec = spec;
         launch_assign_fft(ctx, a, s);
-    } else {
-        a.centroids = C;
-        launch_assign_tc(ctx, a, precision, s);
+        return BOUNDS_OFF;
     }
-    return BOUNDS_OFF;
+    a.centroids = C;
+    const bool usable = bmode != BOUNDS_OFF && bounds_usable(ctx, x, n, m, k, mode, precision);
+    if (!usable) {
+        launch_assign_tc(ctx, a, precision, s);
+        return BOUNDS_OFF;
+    }
+    // BF16 form with bounds: a full pass leaves a lower bound d16 - D on every pair and
+    // per series an upper bound on its best; the tile-bounded pass then evaluates, per
+    // 128-row tile of series grouped by their best centroid, only the centroids whose
+    // bounds do not rule them out for every series of the tile
+    Workspace& ws = ctx->ws;
+    BoundsState& b = bounds_for(ctx, x, n, m, k, mode, precision);
+    int use = bmode == BOUNDS_AUTO ? (b.valid && !b.refresh ? BOUNDS_USE : BOUNDS_REFRESH) : bmode;
+    if (use == BOUNDS_USE && !b.valid) use = BOUNDS_REFRESH;
+    float* lb = ws.bounds.as<float>((size_t)k * n);
+    float* cprev = ws.cprev.as<float>((size_t)k * m + k);
+    float* delta = cprev + (size_t)k * m;
+    char* st = static_cast<char*>(ws.bstate.get((size_t)n * 8));
+    a.ubd = reinterpret_cast<float*>(st);
+    a.jb = reinterpret_cast<int32_t*>(st + (size_t)n * 4);
+    a.lb_out = lb;
+    a.lb_d16 = (float)bf16_error(m, F);
+    launch_centroid_delta(C, k, m, cprev, delta, s);  // cprev <- these centroids
+    if (use == BOUNDS_USE) {
+        unsigned long long* evals = reinterpret_cast<unsigned long long*>(ws.aux.as<char>(64) + 24);
+        TC_CUDA(cudaMemsetAsync(evals, 0, sizeof(unsigned long long), s));
+        TileBounds tb;
+        launch_tile_bounds(ctx, n, m, k, lb, a.ubd, a.jb, delta, a.lb_d16, tb, s);
+        a.perm = tb.perm;
+        a.xbf = tb.xbf;
+        a.xbf_norm = tb.xbf_norm;
+        a.tmask = tb.tmask;
+        a.delta = delta;
+        a.evals = evals;
+    }
+    launch_assign_tc(ctx, a, precision, s);
+    if (use == BOUNDS_REFRESH) {
+        b.valid = true;
+        b.refresh = false;
+    }
+    return use;
 }
 
 // After an assignment that kept bounds: count it, and after a bounded pass rebuild
@@ -160,6 +213,9 @@ static void bounds_feedback(tc_ctx* ctx, int used, unsigned long long evals, int
     if (used == BOUNDS_REFRESH) {
         ++b.screened;
     } else if (used == BOUNDS_USE) {
+        // the FP32 pass counts (series, centroid) pairs, the BF16 pass (tile, centroid)
+        // pairs of its 128-row tiles
+        if (b.precision != TC_PREC_FP32) evals *= 128;
         ++b.bounded;
         b.bounded_pairs += evals;
         b.refresh = (double)evals > BOUNDS_REFRESH_FRACTION * (double)n * k;
@@ -295,6 +351,7 @@ static LoopState run_loop(tc_ctx* ctx, const tc_job* job, const float* x, int k,
     auto readback = [&]() {
         TC_CUDA(cudaMemcpyAsync(&h, aux, sizeof(h), cudaMemcpyDeviceToHost, s));
         TC_CUDA(cudaStreamSynchronize(s));
+        if (h.err[0] || h.err[1]) ctx->bounds.valid = false;  // a pass that stopped early left no bounds
         check_async_errors(h.err);
     };
     TC_CUDA(cudaMemsetAsync(aux, 0, 64, s));
@@ -382,7 +439,7 @@ static const char* const WS_NAMES[] = {"x", "labels", "old_labels", "shift", "di
                                        "seg", "perm", "chunk_counts", "counts", "offsets", "gate", "scal",
                                        "gram", "rowsum", "gram_yt", "gram_poff", "piter", "pstats", "aux",
                                        "toeplitz", "toeplitz_norm", "xbf", "xbf_norm", "first", "gram_sq", "sq_meta", "screen", "gram_part",
-                                       "bounds", "cprev"};
+                                       "bounds", "cprev", "bstate", "bperm", "xbfp", "tmask"};
 
 static std::vector<DevBuf*> workspace_buffers(tc_ctx* ctx);
 
@@ -419,7 +476,7 @@ static std::vector<DevBuf*> workspace_buffers(tc_ctx* ctx) {
             &w.seg,  &w.perm,    &w.chunk_counts, &w.counts, &w.offsets,  &w.gate,      &w.scal,
             &w.gram, &w.rowsum,  &w.gram_yt,    &w.gram_poff, &w.piter,   &w.pstats,    &w.aux,
             &w.toeplitz, &w.toeplitz_norm, &w.xbf, &w.xbf_norm, &w.first, &w.gram_sq, &w.sq_meta, &w.screen, &w.gram_part,
-            &w.bounds, &w.cprev};
+            &w.bounds, &w.cprev, &w.bstate, &w.bperm, &w.xbfp, &w.tmask};
 }
 
 void release_workspace(tc_ctx* ctx) {
@@ -557,6 +614,7 @@ int tc_sbd_assign(tc_ctx* ctx, const float* d_x, const float* d_centroids, int64
         static_assert(sizeof(h) == 32, "aux layout");
         TC_CUDA(cudaMemcpyAsync(&h, aux + 24, sizeof(h), cudaMemcpyDeviceToHost, s));
         TC_CUDA(cudaStreamSynchronize(s));
+        if (h.err[0] || h.err[1]) ctx->bounds.valid = false;  // a pass that stopped early left no bounds
         check_async_errors(h.err);
         bounds_feedback(ctx, used, h.evals, n, k);
     }

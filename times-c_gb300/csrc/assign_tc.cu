@@ -165,7 +165,30 @@ struct AtParams {
     // lower bounds d - lb_d16 on the exact distance of every pair, [n][k] (or null)
     float* lb_out;
     float lb_d16;
+    // per series: an upper bound (best + lb_d16) on the exact distance of its best
+    // centroid, and that centroid (the bounded BF16 pass reads and rewrites them)
+    float* ubd;
+    int32_t* jb;
+    // tile-bounded pass: the tiles hold cluster-grouped positions (perm maps a position
+    // to its series, for the outputs and bounds); only the centroids of tmask[tile]
+    // are evaluated, and the other bounds of the tile's series are carried down by
+    // delta (in place in lb_out)
+    const unsigned long long* tmask;
+    const int32_t* perm;
+    const float* delta;
+    unsigned long long* evals;  // (tile, centroid) pairs evaluated
 };
+
+// The centroids a tile evaluates, in ascending order: all k, or (tile-bounded pass,
+// k <= 64) the bits of its mask.  next_centroid(p, mask, -1) is the first; p.k ends.
+__device__ __forceinline__ unsigned long long tile_mask(const AtParams& p, int64_t tile) {
+    return p.tmask ? p.tmask[tile] : 0ull;
+}
+__device__ __forceinline__ int next_centroid(const AtParams& p, unsigned long long mask, int j) {
+    if (!p.tmask) return j + 1;
+    const unsigned long long rest = j + 1 >= 64 ? 0ull : mask >> (j + 1);
+    return rest ? j + __ffsll((long long)rest) : p.k;
+}
 
 // Keep the list entries with distance <= lim (NaN kept), in order; returns the count.
 // Unrolled with constant indices so the lists stay in registers.
@@ -242,7 +265,8 @@ __global__ void __launch_bounds__(AT_THREADS, 1) k_assign_tc(const __grid_consta
                 sm100::mbar_expect_tx(&a_full, (uint32_t)g.nch * 16384);
                 for (int c = 0; c < g.nch; ++c)
                     sm100::tma_load_2d(Atile + (size_t)c * 16384, &tmapX, 64 * c, (int)(tile * AT_TILE), &a_full);
-                for (int j = 0; j < p.k && ok; ++j)
+                const unsigned long long tmask = tile_mask(p, tile);
+                for (int j = next_centroid(p, tmask, -1); j < p.k && ok; j = next_centroid(p, tmask, j)) {
                     for (int h = 0; h < g.H; ++h, ++q) {
                         const int s = (int)(q & 1), u = (int)(q >> 1);
                         if (u > 0) ok = sm100::mbar_wait(&b_empty[s], (u - 1) & 1, p.err);
@@ -251,6 +275,7 @@ __global__ void __launch_bounds__(AT_THREADS, 1) k_assign_tc(const __grid_consta
                         sm100::bulk_load(Bring + (size_t)s * g.gsz, p.B + j * cent + (size_t)h * g.CPG * g.Lq,
                                          (uint32_t)g.gsz, &b_full[s]);
                     }
+                }
             }
             // copies still in flight land before the CTA can exit: wait for the last
             // phase issued on each barrier (already complete on the normal path)
@@ -284,7 +309,8 @@ __global__ void __launch_bounds__(AT_THREADS, 1) k_assign_tc(const __grid_consta
                 ok = sm100::mbar_wait(&a_full, lt & 1, p.err);
                 if (!ok) break;
                 sm100::tc_fence_after();
-                for (int j = 0; j < p.k && ok; ++j)
+                const unsigned long long tmask = tile_mask(p, tile);
+                for (int j = next_centroid(p, tmask, -1); j < p.k && ok; j = next_centroid(p, tmask, j))
                     for (int h = 0; h < g.H; ++h, ++q) {
                         // ring stage and accumulator slot both follow the group counter
                         const int s = (int)(q & 1);
@@ -320,8 +346,12 @@ __global__ void __launch_bounds__(AT_THREADS, 1) k_assign_tc(const __grid_consta
         int nchg = 0;
         int64_t q = 0;
         for (int64_t tile = blockIdx.x; tile < ntiles && ok; tile += gridDim.x) {
-            const int64_t i = tile * AT_TILE + row;
-            const float xn = i < p.n ? p.xnorm[i] : 0.f;
+            const int64_t pos = tile * AT_TILE + row;  // the tile row (a series position)
+            const int64_t i = pos < p.n ? (p.perm ? (int64_t)p.perm[pos] : pos) : pos;  // its series
+            const float xn = pos < p.n ? p.xnorm[pos] : 0.f;
+            const unsigned long long tmask = tile_mask(p, tile);
+            if (p.evals && p.tmask && warp == 2 && lane == 0)
+                atomicAdd(p.evals, (unsigned long long)__popcll((long long)tmask));
             float bestd = 1e10f;  // get_pos_idx: min_val = 1e10, pos = 0
             int bestj = 0;
             int cj[SCREEN_CAP];
@@ -332,7 +362,7 @@ __global__ void __launch_bounds__(AT_THREADS, 1) k_assign_tc(const __grid_consta
                 cd[t] = 0.f;
             }
             int nc = 0;  // -1: the list overflowed
-            for (int j = 0; j < p.k && ok; ++j) {
+            for (int j = next_centroid(p, tmask, -1); j < p.k && ok; j = next_centroid(p, tmask, j)) {
                 float mx = -3.0e38f;
                 for (int h = 0; h < g.H && ok; ++h, ++q) {
                     const int s = (int)(q & 1);
@@ -367,7 +397,7 @@ __global__ void __launch_bounds__(AT_THREADS, 1) k_assign_tc(const __grid_consta
                 const float ncc = den > 0.f ? mx / den : 0.f;  // a zero norm gives NCC 0 (ncc.cuh:89)
                 float d = 1.0f - ncc;
                 if (p.clamp2 && d > 2.0f) d = 2.0f;
-                if (p.lb_out && i < p.n) p.lb_out[(size_t)i * p.k + j] = __fsub_rd(d, p.lb_d16);
+                if (p.lb_out && pos < p.n) p.lb_out[(size_t)i * p.k + j] = __fsub_rd(d, p.lb_d16);
                 if (d < bestd) {
                     bestd = d;
                     bestj = j;
@@ -387,7 +417,19 @@ __global__ void __launch_bounds__(AT_THREADS, 1) k_assign_tc(const __grid_consta
                     }
                 }
             }
-            if (ok && i < p.n) {
+            if (ok && pos < p.n) {
+                if (p.tmask) {  // the centroids the tile skipped: bounds carried down
+                    float* lr = p.lb_out + (size_t)i * p.k;
+                    const unsigned long long all = p.k >= 64 ? ~0ull : ((1ull << p.k) - 1ull);
+                    for (unsigned long long mk = all & ~tmask; mk; mk &= mk - 1) {
+                        const int j = __ffsll((long long)mk) - 1;
+                        lr[j] = __fsub_rd(lr[j], __ldg(p.delta + j));
+                    }
+                }
+                if (p.ubd) {
+                    p.ubd[i] = __fadd_ru(bestd, p.lb_d16);
+                    p.jb[i] = bestj;
+                }
                 if (p.cand) {
                     if (nc >= 0) nc = screen_compact(cj, cd, nc, bestd + p.thr);
                     int4* o = reinterpret_cast<int4*>(p.cand + (size_t)i * SCREEN_CAP);
@@ -415,6 +457,130 @@ __global__ void __launch_bounds__(AT_THREADS, 1) k_assign_tc(const __grid_consta
     sm100::tc_fence_before();
     __syncthreads();
     if (warp == 0) sm100::tmem_dealloc(tmem, 2 * AT_SLOT_COLS);
+}
+
+// ---------------------------------------------------------------- tile-bounded BF16 pass
+// The series are grouped by the centroid they were last assigned (jb), so that a
+// 128-row tile mostly shares one best centroid and few others can come near it; a
+// tile evaluates a centroid only if one of its series' bounds allows it.  Within a
+// group the order follows the atomics (any order gives the same results).
+
+// a stored best centroid, kept inside [0, k) whatever the buffer holds
+__device__ __forceinline__ int group_of(int j, int k) { return (j >= 0 && j < k) ? j : 0; }
+
+// per-label counts: block histogram in shared memory, one global add per label
+__global__ void k_group_count(const int32_t* __restrict__ jb, int64_t n, int k, int32_t* __restrict__ cnt) {
+    extern __shared__ int32_t hist[];
+    for (int j = threadIdx.x; j < k; j += blockDim.x) hist[j] = 0;
+    __syncthreads();
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) atomicAdd(&hist[group_of(jb[i], k)], 1);
+    __syncthreads();
+    for (int j = threadIdx.x; j < k; j += blockDim.x)
+        if (hist[j]) atomicAdd(&cnt[j], hist[j]);
+}
+
+// cursor[j] = start of group j (exclusive scan of the counts)
+__global__ void k_group_offsets(const int32_t* __restrict__ cnt, int k, int32_t* __restrict__ cursor) {
+    int acc = 0;
+    for (int j = 0; j < k; ++j) {
+        cursor[j] = acc;
+        acc += cnt[j];
+    }
+}
+
+// perm[position] = series: each block reserves a range per label, then places its series
+__global__ void k_group_scatter(const int32_t* __restrict__ jb, int64_t n, int k, int32_t* __restrict__ cursor,
+                                int32_t* __restrict__ perm) {
+    extern __shared__ int32_t hist[];  // [k] counts, then [k] reserved starts
+    for (int j = threadIdx.x; j < 2 * k; j += blockDim.x) hist[j] = 0;
+    __syncthreads();
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    int lab = 0, rank = 0;
+    if (i < n) {
+        lab = group_of(jb[i], k);
+        rank = atomicAdd(&hist[lab], 1);
+    }
+    __syncthreads();
+    for (int j = threadIdx.x; j < k; j += blockDim.x)
+        if (hist[j]) hist[k + j] = atomicAdd(&cursor[j], hist[j]);
+    __syncthreads();
+    if (i < n) perm[hist[k + lab] + rank] = (int32_t)i;
+}
+
+// the BF16 rows and norms in position order (one warp per row, 16-byte copies)
+__global__ void k_permute_bf16(const __nv_bfloat16* __restrict__ xb, const float* __restrict__ xnorm,
+                               const int32_t* __restrict__ perm, int64_t n, int mp, __nv_bfloat16* __restrict__ xbp,
+                               float* __restrict__ normp) {
+    const int lane = threadIdx.x & 31;
+    const int64_t pos = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    if (pos >= n) return;
+    const int64_t i = perm[pos];
+    const int4* src = reinterpret_cast<const int4*>(xb + (size_t)i * mp);
+    int4* dst = reinterpret_cast<int4*>(xbp + (size_t)pos * mp);
+    for (int e = lane; e < mp / 8; e += 32) dst[e] = __ldg(src + e);
+    if (lane == 0) normp[pos] = xnorm[i];
+}
+
+// tmask[tile]: the centroids some series of the tile may have as its minimum.  For
+// series i with best centroid j0, ub = ubd + delta[j0] + D bounds its new BF16
+// distance to j0 from above; centroid j is left out only if lb - delta[j] - D > ub,
+// i.e. its BF16 distance is certainly larger.  j0 is always in.
+__global__ void __launch_bounds__(128) k_tile_masks(const int32_t* __restrict__ perm, const float* __restrict__ lb,
+                                                    const float* __restrict__ ubd, const int32_t* __restrict__ jb,
+                                                    const float* __restrict__ delta, float D, int64_t n, int k,
+                                                    unsigned long long* __restrict__ tmask) {
+    __shared__ unsigned long long part[4];
+    const int64_t pos = (int64_t)blockIdx.x * 128 + threadIdx.x;
+    unsigned long long mask = 0;
+    if (pos < n) {
+        const int64_t i = perm[pos];
+        const int j0 = group_of(jb[i], k);
+        const float ub = __fadd_ru(__fadd_ru(ubd[i], __ldg(delta + j0)), D);
+        mask = 1ull << j0;
+        const float* lr = lb + (size_t)i * k;
+        for (int j = 0; j < k; ++j) {
+            const float l = __fsub_rd(__fsub_rd(lr[j], __ldg(delta + j)), D);
+            if (!(l > ub)) mask |= 1ull << j;
+        }
+    }
+    const unsigned lo = __reduce_or_sync(0xffffffffu, (unsigned)mask);
+    const unsigned hi = __reduce_or_sync(0xffffffffu, (unsigned)(mask >> 32));
+    if ((threadIdx.x & 31) == 0) part[threadIdx.x >> 5] = ((unsigned long long)hi << 32) | lo;
+    __syncthreads();
+    if (threadIdx.x == 0) tmask[blockIdx.x] = part[0] | part[1] | part[2] | part[3];
+}
+
+void launch_tile_bounds(tc_ctx* ctx, int64_t n, int m, int k, const float* lb, const float* ubd, const int32_t* jb,
+                        const float* delta, float D, TileBounds& out, cudaStream_t s) {
+    Workspace& ws = ctx->ws;
+    const int mp = (m + 63) / 64 * 64;
+    const int64_t ntiles = (n + AT_TILE - 1) / AT_TILE;
+    int32_t* perm = ws.bperm.as<int32_t>((size_t)n + 2 * k);
+    int32_t* cnt = perm + n;
+    int32_t* cursor = cnt + k;
+    char* xp = static_cast<char*>(ws.xbfp.get((size_t)n * mp * 2 + (size_t)n * 4 + 16));
+    __nv_bfloat16* xbp = reinterpret_cast<__nv_bfloat16*>(xp);
+    float* normp = reinterpret_cast<float*>(xp + (size_t)n * mp * 2);
+    unsigned long long* tmask = ws.tmask.as<unsigned long long>((size_t)ntiles);
+    const __nv_bfloat16* xb = ws.xbf.as<__nv_bfloat16>((size_t)n * mp);
+    const float* xnorm = ws.xbf_norm.as<float>((size_t)n);
+    TC_CUDA(cudaMemsetAsync(cnt, 0, sizeof(int32_t) * k, s));
+    const int gb = ceil_div(n, 1024);
+    k_group_count<<<gb, 1024, sizeof(int32_t) * k, s>>>(jb, n, k, cnt);
+    TC_CHECK_LAUNCH();
+    k_group_offsets<<<1, 1, 0, s>>>(cnt, k, cursor);
+    TC_CHECK_LAUNCH();
+    k_group_scatter<<<gb, 1024, sizeof(int32_t) * 2 * k, s>>>(jb, n, k, cursor, perm);
+    TC_CHECK_LAUNCH();
+    k_permute_bf16<<<ceil_div(n * 32, 256), 256, 0, s>>>(xb, xnorm, perm, n, mp, xbp, normp);
+    TC_CHECK_LAUNCH();
+    k_tile_masks<<<(unsigned)ntiles, 128, 0, s>>>(perm, lb, ubd, jb, delta, D, n, k, tmask);
+    TC_CHECK_LAUNCH();
+    out.perm = perm;
+    out.xbf = xbp;
+    out.xbf_norm = normp;
+    out.tmask = tmask;
 }
 
 // ---------------------------------------------------------------- host
@@ -506,8 +672,9 @@ void launch_assign_tc(tc_ctx* ctx, const AssignArgs& a, int precision, cudaStrea
         prepare_series_bf16(ctx, a.x, a.n, a.m, s);
         ctx->prep_x = nullptr;  // converted for this call only: the caller may change x
     }
-    __nv_bfloat16* xb = ws.xbf.as<__nv_bfloat16>((size_t)a.n * g.mp);
-    float* xnorm = ws.xbf_norm.as<float>((size_t)a.n);
+    const __nv_bfloat16* xb = a.xbf ? static_cast<const __nv_bfloat16*>(a.xbf)
+                                    : ws.xbf.as<__nv_bfloat16>((size_t)a.n * g.mp);
+    const float* xnorm = a.xbf ? a.xbf_norm : ws.xbf_norm.as<float>((size_t)a.n);
     __nv_bfloat16* B = ws.toeplitz.as<__nv_bfloat16>((size_t)a.k * g.NBT * g.Lq);
     float* cnorm = ws.toeplitz_norm.as<float>((size_t)a.k);
     k_centroid_toeplitz<<<a.k, 256, 0, s>>>(a.centroids, a.m, a.F, g.Lq, B, cnorm);
@@ -530,11 +697,17 @@ void launch_assign_tc(tc_ctx* ctx, const AssignArgs& a, int precision, cudaStrea
     p.changed = a.changed;
     p.dist_sum = a.dist_sum;
     p.err = err;
+    p.lb_out = a.lb_out;
+    p.lb_d16 = a.lb_d16;
+    p.ubd = a.ubd;
+    p.jb = a.jb;
+    p.tmask = a.tmask;
+    p.perm = a.perm;
+    p.delta = a.delta;
+    p.evals = a.evals;
     if (a.cand) {
         p.cand = a.cand;
         p.ncand = a.ncand;
-        p.lb_out = a.lb_out;
-        p.lb_d16 = a.lb_d16;
         p.thr = screen_threshold(a.m, a.F);
         p.labels = nullptr;
         p.dist = nullptr;

@@ -204,6 +204,11 @@ uint64_t tc_job_footprint(const tc_job* j) {
         b += k * (F / 8) * (mp + 56) * 2 + k * 4;  // shifted centroid buffers
     }
     if (screened) b += n * (tc::SCREEN_CAP + 1) * 4 + k * n * 4 + (k * m + k) * 4;  // candidates, bounds
+    if (j->precision == TC_PREC_BF16 && tc::tc_assign_supported(j->m, (int)F, j->k, j->precision) && k <= 64) {
+        const uint64_t mp = (m + 63) / 64 * 64;
+        b += k * n * 4 + (k * m + k) * 4 + n * 12 + 2 * k * 4;  // bounds, best bounds, grouping
+        b += n * mp * 2 + n * 4 + ((n + 127) / 128) * 8;        // grouped BF16 copy, tile masks
+    }
     b += ((n + 4095) / 4096) * k * 4;      // segment chunk counts
     return b + (1u << 20);
 }

@@ -142,6 +142,10 @@ struct Workspace {
     DevBuf screen;       // n x SCREEN_CAP candidate centroids + n counts (screened FP32 assignment)
     DevBuf bounds;       // n x k f32: distance lower bounds (bounded assignment)
     DevBuf cprev;        // k x m f32 unit centroids the bounds refer to, + k f32 movements
+    DevBuf bstate;       // n f32 + n i32: per series the best centroid's upper bound and index (BF16 bounds)
+    DevBuf bperm;        // n i32 positions -> series, + 2k i32 group counts and cursors
+    DevBuf xbfp;         // n x mp bf16 + n f32: the BF16 series and norms in position order
+    DevBuf tmask;        // one u64 centroid mask per 128-row tile
 };
 
 // State of the bounded assignment across iterations: the bounds in ws.bounds are
@@ -149,7 +153,7 @@ struct Workspace {
 struct BoundsState {
     const float* x = nullptr;
     int64_t n = 0;
-    int m = 0, k = 0, mode = -1;
+    int m = 0, k = 0, mode = -1, precision = -1;
     bool valid = false;
     bool refresh = true;  // next assignment: the screened pass (new bounds)
     // totals for tc_assign_stats
@@ -222,6 +226,16 @@ struct AssignArgs {
     float lb_eps;   // bound on |d32 - d| of the FFT kernel (fft_error)
     float lb_d16;   // bound on |d16 - d| of the tensor-core pass
     unsigned long long* evals;  // bounded pass: pairs evaluated (accumulated)
+    // tensor-core pass with bounds (BF16 form): per series an upper bound on the exact
+    // distance of its best centroid and that centroid; the tile-bounded pass also
+    // takes the series in position order (xbf, xbf_norm, perm) and a centroid mask
+    // per 128-row tile
+    float* ubd;
+    int32_t* jb;
+    const void* xbf;
+    const float* xbf_norm;
+    const int32_t* perm;
+    const unsigned long long* tmask;
 };
 void launch_assign_fft(tc_ctx* ctx, const AssignArgs& a, cudaStream_t s);
 // movement of every centroid since cprev (unit vectors, k x m), then cprev <- the unit
@@ -245,6 +259,17 @@ void prepare_series_bf16_reserve(tc_ctx* ctx, int64_t n, int m);
 void prepare_series_bf16_rows(tc_ctx* ctx, const float* x, int64_t n, int m, int64_t r0, int64_t rows,
                               cudaStream_t s);
 void prepare_series_bf16_done(tc_ctx* ctx, const float* x, int64_t n, int m);
+// The tile-bounded BF16 pass's inputs: series grouped by their best centroid jb
+// (perm: position -> series), their BF16 rows and norms in that order, and per
+// 128-row tile the centroids a series of the tile may have as its minimum (k <= 64).
+struct TileBounds {
+    const int32_t* perm = nullptr;
+    const void* xbf = nullptr;
+    const float* xbf_norm = nullptr;
+    const unsigned long long* tmask = nullptr;
+};
+void launch_tile_bounds(tc_ctx* ctx, int64_t n, int m, int k, const float* lb, const float* ubd, const int32_t* jb,
+                        const float* delta, float D, TileBounds& out, cudaStream_t s);
 
 // extraction
 struct ExtractArgs {
