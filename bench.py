@@ -308,19 +308,53 @@ def ari(a, b):
 
 
 def bf16_assign_ms(ctx, x, C, k, mode, stream, reps=3):
-    """CUDA-event time of the BF16 tensor-core assignment on these series (outputs to scratch)."""
+    """CUDA-event time of the full BF16 tensor-core assignment on these series (every
+    pair evaluated: distance bounds off; outputs to scratch)."""
     import torch
     n = x.shape[0]
     lab = torch.zeros(n, dtype=torch.int32, device="cuda")
     dist = torch.zeros(n, dtype=torch.float32, device="cuda")
-    ctx.sbd_assign(x, C, mode=mode, precision=PREC["bf16"], labels=lab, dist=dist, stream=stream)
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    e0.record(stream)
-    for _ in range(reps):
+    os.environ["TIMESC_NO_BOUNDS"] = "1"
+    try:
         ctx.sbd_assign(x, C, mode=mode, precision=PREC["bf16"], labels=lab, dist=dist, stream=stream)
-    e1.record(stream)
-    torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(reps):
+            ctx.sbd_assign(x, C, mode=mode, precision=PREC["bf16"], labels=lab, dist=dist, stream=stream)
+        e1.record(stream)
+        torch.cuda.synchronize()
+    finally:
+        del os.environ["TIMESC_NO_BOUNDS"]
     return e0.elapsed_time(e1) / reps
+
+
+def dense_iterations(ctx, x, labels, C, n, k, mode, prec, stream, steps):
+    """The same iterations from the same state with the distance bounds off (every pair
+    evaluated): ms per whole iteration and per assignment, for comparison."""
+    import torch
+    lab = labels.clone()
+    old = labels.clone()
+    Cw = C.clone()
+    dist = torch.empty((n,), dtype=torch.float32, device="cuda")
+    ch = torch.zeros(1, dtype=torch.int32, device="cuda")
+    e0, e1, a0, a1 = (torch.cuda.Event(enable_timing=True) for _ in range(4))
+    os.environ["TIMESC_NO_BOUNDS"] = "1"
+    try:
+        a_tot = 0.0
+        e0.record(stream)
+        for _ in range(steps):
+            ctx.extract_shapes(x, lab, Cw, mode=mode, precision=prec)
+            ch.zero_()
+            a0.record(stream)
+            ctx.sbd_assign(x, Cw, mode=mode, precision=prec, labels=lab, dist=dist, old_labels=old, changed=ch)
+            a1.record(stream)
+            ch.item()
+            a_tot += a0.elapsed_time(a1)
+        e1.record(stream)
+        torch.cuda.synchronize()
+    finally:
+        del os.environ["TIMESC_NO_BOUNDS"]
+    return e0.elapsed_time(e1) / steps, a_tot / steps
 
 
 def plain_fp32_compare(ctx, x, labels, C, n, m, k, mode, prec, stream, ms_mixed, a_ms_mixed, steps=2):
@@ -330,8 +364,8 @@ def plain_fp32_compare(ctx, x, labels, C, n, m, k, mode, prec, stream, ms_mixed,
     distance error, label agreement and ARI)."""
     import torch
     lab0 = labels.clone()
-    C32 = torch.empty_like(C)
-    C16 = torch.empty_like(C)
+    C32 = C.clone()  # the extraction aligns members to the centroids it is given
+    C16 = C.clone()
     ctx.extract_shapes(x, lab0, C32, mode=mode, precision=PREC["fp32"])
     ctx.extract_shapes(x, lab0, C16, mode=mode, precision=prec)
     l32 = torch.empty_like(labels)
@@ -615,6 +649,8 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-cufft", action="store_true")
+    ap.add_argument("--no-compare", action="store_true",
+                    help="leave out the plain FP32 form and dense comparisons (the timed loop is unchanged)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     if args.precision is None:
@@ -676,7 +712,9 @@ def main():
     if dist:
         dist.barrier()
     torch.cuda.synchronize()
+    snap = (labels.clone(), C.clone())  # the state the timed iterations start from
     clk.begin()
+    st0 = ctx.assign_stats()
     l0 = timesc.lib().tc_launch_count()
     t_start = torch.cuda.Event(enable_timing=True)
     t_end = torch.cuda.Event(enable_timing=True)
@@ -687,6 +725,7 @@ def main():
     torch.cuda.synchronize()
     clk.end()
     launches = timesc.lib().tc_launch_count() - l0
+    st1 = ctx.assign_stats()
     clocks = clk.stop()
     ms = t_start.elapsed_time(t_end)
     assign_ms = [a.elapsed_time(b) for a, b in ev]
@@ -705,8 +744,12 @@ def main():
         achieved_gbs = nbytes / (a_ms / 1e3) / 1e9
         sm_mhz = clocks.get("sm_mhz") or 2070.0
         fp32_peak = 152 * 128 * 2 * sm_mhz * 1e6 / 1e12
+        full_full, full_bnd, pairs_bnd = (b - a for a, b in zip(st0, st1))
         if tc_supported(m, F, prec):
-            tflops = tc_flops(n, m, k, F) / (a_ms / 1e3) / 1e12
+            # the kernel at full work (every pair), timed on its own; the timed iterations
+            # mostly run the bounded pass (see "bounds")
+            t_full = bf16_assign_ms(ctx, x, C, k, mode, stream)
+            tflops = tc_flops(n, m, k, F) / (t_full / 1e3) / 1e12
             mp = (m + 63) // 64 * 64
             tc_bytes = 2 * n * mp + 8 * n + 2 * k * (F // 8) * (mp + 56)  # BF16 series, labels+dist, buffers
             nominal = bf16_nominal_tflops(sm_mhz)
@@ -716,11 +759,12 @@ def main():
                     "peak_source": peak_kind + " (cuBLAS bf16 burst); the kernel can exceed it: it holds "
                                    "a higher clock than the power-capped cuBLAS run",
                     "nominal_at_median_clock": nominal, "frac_of_nominal": tflops / nominal,
-                    "algorithmic_flops_per_launch": tc_flops(n, m, k, F), "launch_ms": a_ms,
-                    "hbm": {"achieved": tc_bytes / (a_ms / 1e3) / 1e9, "peak": hbm,
+                    "algorithmic_flops_per_launch": tc_flops(n, m, k, F), "launch_ms": t_full,
+                    "hbm": {"achieved": tc_bytes / (t_full / 1e3) / 1e9, "peak": hbm,
                             "algorithmic_bytes_per_launch": tc_bytes},
-                    "note": "launch_ms covers the shifted centroid buffers and the correlation kernel; the "
-                            "BF16 copy of the (fixed) series is made once per run (tc_prepare_series)"}
+                    "note": "a full assignment (every pair, distance bounds off) timed on its own: launch_ms "
+                            "covers the shifted centroid buffers and the correlation kernel; the BF16 copy of "
+                            "the (fixed) series is made once per run (tc_prepare_series)"}
         elif screened(m, F, k, prec):
             # the screening pass alone: the same tensor-core kernel as the BF16 assignment
             tc_ms = bf16_assign_ms(ctx, x, C, k, mode, stream)
@@ -760,10 +804,23 @@ def main():
                "config": arm_config(args, wl, F, world),
                "kshape_iters_per_s": 1e3 / ms_step,
                "assign_pairs_per_s": n * k / (a_ms / 1e3),
+               "assign_ms": a_ms,
                "roofline": roof, "gpu_launches": int(launches), "clocks": clocks}
+        if full_bnd and not args.no_compare:
+            dense_ms, dense_a = dense_iterations(ctx, x, snap[0], snap[1], n, k, mode, prec, stream, args.steps)
+            out["bounds"] = {
+                "full_passes": int(full_full), "bounded_passes": int(full_bnd),
+                "evaluated_fraction_in_bounded_passes": pairs_bnd / (full_bnd * n * k),
+                "evaluated_fraction_all_timed": (pairs_bnd + full_full * n * k) / (args.steps * n * k),
+                "dense_ms_per_iteration": dense_ms, "dense_assign_ms": dense_a,
+                "speedup_vs_dense_iteration": dense_ms / ms_step,
+                "what": "the assignment keeps lower bounds on every (series, centroid) distance across "
+                        "iterations and evaluates only the pairs they do not rule out (labels and distances "
+                        "equal to evaluating every pair, tested bit for bit); value counts every pair "
+                        "decided; dense_*: the same iterations from the same state with the bounds off"}
 
     # the plain FP32 form on the same series, and the mixed form's agreement with it
-    if out is not None and prec != PREC["fp32"]:
+    if out is not None and prec != PREC["fp32"] and not args.no_compare:
         out["plain_fp32_fused"] = plain_fp32_compare(ctx, x, labels, C, n, m, k, mode, prec, stream,
                                                      ms_step, a_ms)
 

@@ -94,10 +94,10 @@ int tc_init_labels(tc_ctx* ctx, int32_t* d_labels, int64_t n, int k, tc_stream s
  * smallest distance), d_shift (the shift that aligns the series to its centroid:
  * out[t] = x[t - shift]).  If d_old_labels is not NULL, *d_changed receives the
  * number of labels that differ from it; d_dist_sum receives the FP64 sum of
- * d_dist (both accumulated: zero them first).  With TC_PREC_FP32 on prepared series
- * (tc_prepare_series) a call may use the distance bounds kept from earlier calls
- * (tc_assign_stats); it then reads d_labels first, as the series' most likely
- * centroid - any contents give the same results. */
+ * d_dist (both accumulated: zero them first).  On prepared series (tc_prepare_series)
+ * a call may use the distance bounds kept from earlier calls (tc_assign_stats); in
+ * TC_PREC_FP32 it then reads d_labels first, as the series' most likely centroid -
+ * any contents give the same results, the previous labels the fewest evaluations. */
 int tc_sbd_assign(tc_ctx* ctx, const float* d_x, const float* d_centroids, int64_t n, int m, int k,
                   int mode, int precision, int32_t* d_labels, float* d_dist, int32_t* d_shift,
                   const int32_t* d_old_labels, int32_t* d_changed, double* d_dist_sum,
@@ -111,15 +111,20 @@ int tc_sbd_assign(tc_ctx* ctx, const float* d_x, const float* d_centroids, int64
  * the reference (NCC_3D transforms the series on every iteration). */
 int tc_prepare_series(tc_ctx* ctx, const float* d_x, int64_t n, int m, tc_stream stream);
 
-/* Work of the FP32 assignments on this context since its creation.  On series kept
- * fixed across calls (tc_prepare_series, and inside tc_kshape_run) the FP32
- * assignment keeps lower bounds on every (series, centroid) distance: a screened
- * call (the BF16 tensor-core pass and the FP32 pass over its candidates) builds
- * them, and later calls carry them over with each centroid's movement and evaluate
- * only the pairs whose bound does not rule them out - with labels and distances
- * equal to evaluating every pair.  screened: calls that built bounds; bounded: calls
- * that used them; bounded_pairs: pairs those evaluated (out of n*k each).  Any
- * output may be NULL.  No counterpart in the reference. */
+/* Work of the assignments on this context since its creation.  On series kept
+ * fixed across calls (tc_prepare_series, and inside tc_kshape_run) the assignment
+ * keeps lower bounds on every (series, centroid) distance, in both precision forms
+ * at FFT lengths 128..1024 (m <= 512): a full call builds them (in TC_PREC_FP32 the
+ * screened call: the BF16 tensor-core pass and the FP32 pass over its candidates),
+ * and later calls carry them over with each centroid's movement and evaluate only
+ * the pairs whose bound does not rule them out - per series in TC_PREC_FP32, per
+ * 128-series tile of series grouped by their best centroid in TC_PREC_BF16 - with
+ * labels and distances equal to evaluating every pair.  A call that evaluated more
+ * than 30% of its pairs makes the next one a full call.  screened: calls that built
+ * bounds; bounded: calls that used them; bounded_pairs: pairs those evaluated (out
+ * of n*k each; whole 128-series tiles in TC_PREC_BF16).  Any output may be NULL.
+ * TIMESC_NO_BOUNDS=1 in the environment turns the bounds off.  No counterpart in
+ * the reference. */
 int tc_assign_stats(const tc_ctx* ctx, uint64_t* screened, uint64_t* bounded, uint64_t* bounded_pairs);
 
 /* Allocation-free SBD assignment.  No counterpart in the reference.
