@@ -95,9 +95,8 @@ int tc_init_labels(tc_ctx* ctx, int32_t* d_labels, int64_t n, int k, tc_stream s
  * out[t] = x[t - shift]).  If d_old_labels is not NULL, *d_changed receives the
  * number of labels that differ from it; d_dist_sum receives the FP64 sum of
  * d_dist (both accumulated: zero them first).  On prepared series (tc_prepare_series)
- * a call may use the distance bounds kept from earlier calls (tc_assign_stats); in
- * TC_PREC_FP32 it then reads d_labels first, as the series' most likely centroid -
- * any contents give the same results, the previous labels the fewest evaluations. */
+ * a call may use the distance bounds kept from earlier calls (tc_assign_stats), with
+ * the same results. */
 int tc_sbd_assign(tc_ctx* ctx, const float* d_x, const float* d_centroids, int64_t n, int m, int k,
                   int mode, int precision, int32_t* d_labels, float* d_dist, int32_t* d_shift,
                   const int32_t* d_old_labels, int32_t* d_changed, double* d_dist_sum,
@@ -117,15 +116,24 @@ int tc_prepare_series(tc_ctx* ctx, const float* d_x, int64_t n, int m, tc_stream
  * at FFT lengths 128..1024 (m <= 512): a full call builds them (in TC_PREC_FP32 the
  * screened call: the BF16 tensor-core pass and the FP32 pass over its candidates),
  * and later calls carry them over with each centroid's movement and evaluate only
- * the pairs whose bound does not rule them out - per series in TC_PREC_FP32, per
- * 128-series tile of series grouped by their best centroid in TC_PREC_BF16 - with
- * labels and distances equal to evaluating every pair.  A call that evaluated more
+ * the pairs whose bound does not rule them out, per 128-series tile of series
+ * grouped by their best centroid (in TC_PREC_FP32 that tile-bounded BF16 pass is the
+ * screen, and the FP32 pass evaluates its candidates) - with labels and distances
+ * equal to evaluating every pair.  A call that evaluated more
  * than 30% of its pairs makes the next one a full call.  screened: calls that built
  * bounds; bounded: calls that used them; bounded_pairs: pairs those evaluated (out
- * of n*k each; whole 128-series tiles in TC_PREC_BF16).  Any output may be NULL.
+ * of n*k each, counted in whole 128-series tiles).  Any output may be NULL.
  * TIMESC_NO_BOUNDS=1 in the environment turns the bounds off.  No counterpart in
  * the reference. */
 int tc_assign_stats(const tc_ctx* ctx, uint64_t* screened, uint64_t* bounded, uint64_t* bounded_pairs);
+
+/* Work the extraction memo saved on this context since its creation: extractions
+ * that compared their clusters with the previous call's (prepared series, and
+ * every extraction inside tc_kshape_run except the repeated-squaring forms),
+ * clusters they covered, and clusters whose output was reused instead of
+ * recomputed.  Synchronises the device.  Any output may be NULL.  No counterpart in
+ * the reference. */
+int tc_extract_stats(tc_ctx* ctx, uint64_t* extractions, uint64_t* clusters, uint64_t* reused);
 
 /* Allocation-free SBD assignment.  No counterpart in the reference.
  * For callers that must not allocate device memory on the call path: a serving
@@ -153,7 +161,11 @@ int tc_sbd_assign_noalloc(const float* d_x, const float* d_centroids, int64_t n,
  * cal_select = 1 takes the fully converged top eigenvector (the reference's
  * syevd path).  Empty clusters keep their centroid.  d_counts (k, may be NULL)
  * receives the cluster sizes and *h_sum_class (may be NULL) the number of
- * non-empty clusters (this synchronises the stream). */
+ * non-empty clusters (this synchronises the stream).  On prepared series
+ * (tc_prepare_series) without d_shift, a cluster whose members and centroid equal
+ * those of the previous call on this context gets that call's output again
+ * without being recomputed - the same bits, as every stage is deterministic per
+ * cluster (tc_extract_stats; TIMESC_NO_MEMO=1 turns it off). */
 int tc_extract_shapes(tc_ctx* ctx, const float* d_x, const int32_t* d_labels, const int32_t* d_shift,
                       float* d_centroids, int64_t n, int m, int k, int mode, int cal_select,
                       int precision, int32_t* d_counts, int* h_sum_class, tc_stream stream);

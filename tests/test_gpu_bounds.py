@@ -4,10 +4,11 @@ labels, distances and centroids of evaluating every pair.
 On series kept fixed across calls (tc_prepare_series, and inside tc_kshape_run)
 a full assignment leaves a lower bound on every (series, centroid) distance; the
 next assignments lower each bound by its centroid's movement and evaluate only
-the pairs the bounds do not rule out - per series in the FP32 form (previous
-label first), per 128-row tile of series grouped by their best centroid in the
-BF16 form.  TIMESC_NO_BOUNDS=1 turns that off: both runs must agree bit for bit,
-on ordinary data, exact ties, a zero centroid and a centroid that flips sign.
+the pairs the bounds do not rule out, per 128-row tile of series grouped by their
+best centroid (in the FP32 form that bounded BF16 pass is the screen and the FFT
+kernel evaluates its candidates).  TIMESC_NO_BOUNDS=1 turns that off: both runs
+must agree bit for bit, on ordinary data, exact ties, a zero centroid and a
+centroid that flips sign.
 """
 import os
 
@@ -63,8 +64,8 @@ def test_loop_with_bounds_equals_dense(built, prec, mode, n, m, k, init_chose):
 def test_stage_calls_with_bounds_ties_zero_and_flip(built, prec):
     """Stage calls on prepared series: each call with bounds against a context that
     evaluates every pair, over a sequence of centroid sets with small moves, an exact
-    duplicate (ties go to the first index even when the previous label is the later
-    one), a zero centroid appearing and disappearing, and a sign flip."""
+    duplicate (ties go to the first index even when the labels passed in name the
+    later one), a zero centroid appearing and disappearing, and a sign flip."""
     import torch
     T, O = built
     n, m, k = 6000, 256, 8
@@ -96,7 +97,7 @@ def test_stage_calls_with_bounds_ties_zero_and_flip(built, prec):
         for step, C in enumerate(seq):
             cg = torch.from_numpy(np.ascontiguousarray(C)).cuda()
             if step == 2:
-                lab_b.fill_(5)  # previous label the later duplicate: the first index must still win
+                lab_b.fill_(5)  # labels in naming the later duplicate: the first index must still win
             db = torch.zeros(n, dtype=torch.float32, device="cuda")
             dd = torch.zeros(n, dtype=torch.float32, device="cuda")
             ctx_b.sbd_assign(x, cg, mode=0, precision=prec, labels=lab_b, dist=db)

@@ -65,8 +65,10 @@ constexpr double BOUNDS_REFRESH_FRACTION = 0.3;
 // form where the tensor-core correlation runs with k <= 64 (one mask word per tile).
 static bool bounds_usable(const tc_ctx* ctx, const float* x, int64_t n, int m, int k, int mode, int precision) {
     const int F = fft_size(m, mode);
-    const bool form = precision == TC_PREC_FP32 ? screen_supported(m, F, k)
-                                                : (tc_assign_supported(m, F, k, precision) && k >= 2 && k <= 64);
+    // both forms bound through the tensor-core pass's 64-bit tile masks
+    const bool form = (precision == TC_PREC_FP32 ? screen_supported(m, F, k)
+                                                 : tc_assign_supported(m, F, k, precision)) &&
+                      k >= 2 && k <= 64;
     return form && !std::getenv("TIMESC_NO_BOUNDS") && ctx->prep_x == x && ctx->prep_n == n && ctx->prep_m == m;
 }
 
@@ -108,47 +110,54 @@ static int assign(tc_ctx* ctx, const float* x, const float* C, int64_t n, int m,
     a.changed = changed;
     a.dist_sum = dsum;
     if (precision == TC_PREC_FP32 && !shift && screen_supported(m, F, k)) {
+        // exact screening: the BF16 pass keeps every centroid whose FP32 distance can be
+        // the minimum, the FP32 pass evaluates those (same labels and distances as the
+        // unscreened FP32 kernel).  With bounds, the BF16 pass is the tile-bounded one
+        // (as in the BF16 form): a centroid its tile leaves out has an exact distance
+        // above the series' best by more than 2D >= 2 eps, so it is not the FP32 first
+        // minimum either, and among the centroids it evaluates the screen keeps that
+        // minimum as before.
         Workspace& ws = ctx->ws;
         const bool usable = bmode != BOUNDS_OFF && bounds_usable(ctx, x, n, m, k, mode, precision);
         BoundsState& b = usable ? bounds_for(ctx, x, n, m, k, mode, precision) : ctx->bounds;
         int use = BOUNDS_OFF;
         if (usable) use = bmode == BOUNDS_AUTO ? (b.valid && !b.refresh ? BOUNDS_USE : BOUNDS_REFRESH) : bmode;
         if (use == BOUNDS_USE && !b.valid) use = BOUNDS_REFRESH;
-        float *lb = nullptr, *delta = nullptr;
-        unsigned long long* evals = reinterpret_cast<unsigned long long*>(ws.aux.as<char>(64) + 24);
-        if (use != BOUNDS_OFF) {
-            lb = ws.bounds.as<float>((size_t)k * n);
-            float* cprev = ws.cprev.as<float>((size_t)k * m + k);
-            delta = cprev + (size_t)k * m;
-            launch_centroid_delta(C, k, m, cprev, delta, s);  // cprev <- these centroids
-            a.lb_eps = (float)(fft_error(m, F) + 1e-6);
-            TC_CUDA(cudaMemsetAsync(evals, 0, sizeof(unsigned long long), s));
-        }
-        float2* spec = ws.spectra.as<float2>((size_t)k * (F / 2 + 1));
-        launch_centroid_spectra(ctx, C, k, m, F, spec, s);
-        a.spec = spec;
-        if (use == BOUNDS_USE) {
-            a.lb_in = lb;
-            a.lb_out = lb;  // updated in place
-            a.delta = delta;
-            a.evals = evals;
-            launch_assign_fft(ctx, a, s);
-            return use;
-        }
-        // exact screening: the BF16 pass keeps every centroid whose FP32 distance can be
-        // the minimum, the FP32 pass evaluates those (same labels and distances as the
-        // unscreened FP32 kernel); with bounds, both write theirs for every pair
         a.centroids = C;
         a.cand = ws.screen.as<int32_t>((size_t)n * (SCREEN_CAP + 1));
         a.ncand = a.cand + (size_t)n * SCREEN_CAP;
-        if (use == BOUNDS_REFRESH) {
-            a.lb_out = lb;
+        if (use != BOUNDS_OFF) {
+            float* cprev = ws.cprev.as<float>((size_t)k * m + k);
+            float* delta = cprev + (size_t)k * m;
+            launch_centroid_delta(C, k, m, cprev, delta, s);  // cprev <- these centroids
+            char* st = static_cast<char*>(ws.bstate.get((size_t)n * 12));
+            a.ubd = reinterpret_cast<float*>(st);
+            a.jb = reinterpret_cast<int32_t*>(st + (size_t)n * 4);
+            if (use == BOUNDS_REFRESH) a.gkey = reinterpret_cast<int32_t*>(st + (size_t)n * 8);
+            a.lb_out = ws.bounds.as<float>((size_t)k * n);  // the BF16 pass d16 - D, the FP32 pass d32 - eps
             a.lb_d16 = (float)bf16_error(m, F);
+            a.lb_eps = (float)(fft_error(m, F) + 1e-6);
+            if (use == BOUNDS_USE) {
+                unsigned long long* evals = reinterpret_cast<unsigned long long*>(ws.aux.as<char>(64) + 24);
+                TC_CUDA(cudaMemsetAsync(evals, 0, sizeof(unsigned long long), s));
+                TileBounds tb;
+                launch_tile_masks(ctx, n, m, k, a.lb_out, a.ubd, a.jb, delta, a.lb_d16, tb, s);
+                a.perm = tb.perm;
+                a.xbf = tb.xbf;
+                a.xbf_norm = tb.xbf_norm;
+                a.tmask = tb.tmask;
+                a.delta = delta;
+                a.evals = evals;
+            }
         }
         // -1 (all centroids) for every series the tensor-core pass does not reach,
         // e.g. after one of its bounded waits ran out
         TC_CUDA(cudaMemsetAsync(a.ncand, 0xFF, (size_t)n * sizeof(int32_t), s));
         launch_assign_tc(ctx, a, TC_PREC_BF16, s);
+        if (use == BOUNDS_REFRESH) launch_tile_group(ctx, n, m, k, a.gkey, s);
+        float2* spec = ws.spectra.as<float2>((size_t)k * (F / 2 + 1));
+        launch_centroid_spectra(ctx, C, k, m, F, spec, s);
+        a.spec = spec;
         launch_assign_fft(ctx, a, s);
         if (use == BOUNDS_REFRESH) {
             b.valid = true;
@@ -170,9 +179,9 @@ static int assign(tc_ctx* ctx, const float* x, const float* C, int64_t n, int m,
         return BOUNDS_OFF;
     }
     // BF16 form with bounds: a full pass leaves a lower bound d16 - D on every pair and
-    // per series an upper bound on its best; the tile-bounded pass then evaluates, per
-    // 128-row tile of series grouped by their best centroid, only the centroids whose
-    // bounds do not rule them out for every series of the tile
+    // per series an upper bound on its best, and groups the series by that best; the
+    // tile-bounded passes then evaluate, per 128-row tile of that grouping, only the
+    // centroids whose bounds do not rule them out for every series of the tile
     Workspace& ws = ctx->ws;
     BoundsState& b = bounds_for(ctx, x, n, m, k, mode, precision);
     int use = bmode == BOUNDS_AUTO ? (b.valid && !b.refresh ? BOUNDS_USE : BOUNDS_REFRESH) : bmode;
@@ -180,9 +189,10 @@ static int assign(tc_ctx* ctx, const float* x, const float* C, int64_t n, int m,
     float* lb = ws.bounds.as<float>((size_t)k * n);
     float* cprev = ws.cprev.as<float>((size_t)k * m + k);
     float* delta = cprev + (size_t)k * m;
-    char* st = static_cast<char*>(ws.bstate.get((size_t)n * 8));
+    char* st = static_cast<char*>(ws.bstate.get((size_t)n * 12));
     a.ubd = reinterpret_cast<float*>(st);
     a.jb = reinterpret_cast<int32_t*>(st + (size_t)n * 4);
+    if (use == BOUNDS_REFRESH) a.gkey = reinterpret_cast<int32_t*>(st + (size_t)n * 8);
     a.lb_out = lb;
     a.lb_d16 = (float)bf16_error(m, F);
     launch_centroid_delta(C, k, m, cprev, delta, s);  // cprev <- these centroids
@@ -190,7 +200,7 @@ static int assign(tc_ctx* ctx, const float* x, const float* C, int64_t n, int m,
         unsigned long long* evals = reinterpret_cast<unsigned long long*>(ws.aux.as<char>(64) + 24);
         TC_CUDA(cudaMemsetAsync(evals, 0, sizeof(unsigned long long), s));
         TileBounds tb;
-        launch_tile_bounds(ctx, n, m, k, lb, a.ubd, a.jb, delta, a.lb_d16, tb, s);
+        launch_tile_masks(ctx, n, m, k, lb, a.ubd, a.jb, delta, a.lb_d16, tb, s);
         a.perm = tb.perm;
         a.xbf = tb.xbf;
         a.xbf_norm = tb.xbf_norm;
@@ -200,6 +210,10 @@ static int assign(tc_ctx* ctx, const float* x, const float* C, int64_t n, int m,
     }
     launch_assign_tc(ctx, a, precision, s);
     if (use == BOUNDS_REFRESH) {
+        // the bounded passes until the next full one keep this grouping (by best and
+        // second best: series with both in common have similar masks); a series whose
+        // best centroid changes stays in its tile, which only widens that tile's mask
+        launch_tile_group(ctx, n, m, k, a.gkey, s);
         b.valid = true;
         b.refresh = false;
     }
@@ -213,9 +227,8 @@ static void bounds_feedback(tc_ctx* ctx, int used, unsigned long long evals, int
     if (used == BOUNDS_REFRESH) {
         ++b.screened;
     } else if (used == BOUNDS_USE) {
-        // the FP32 pass counts (series, centroid) pairs, the BF16 pass (tile, centroid)
-        // pairs of its 128-row tiles
-        if (b.precision != TC_PREC_FP32) evals *= 128;
+        // the tensor-core pass counts (tile, centroid) pairs of its 128-row tiles
+        evals *= 128;
         ++b.bounded;
         b.bounded_pairs += evals;
         b.refresh = (double)evals > BOUNDS_REFRESH_FRACTION * (double)n * k;
@@ -351,7 +364,10 @@ static LoopState run_loop(tc_ctx* ctx, const tc_job* job, const float* x, int k,
     auto readback = [&]() {
         TC_CUDA(cudaMemcpyAsync(&h, aux, sizeof(h), cudaMemcpyDeviceToHost, s));
         TC_CUDA(cudaStreamSynchronize(s));
-        if (h.err[0] || h.err[1]) ctx->bounds.valid = false;  // a pass that stopped early left no bounds
+        if (h.err[0] || h.err[1]) {  // a pass that stopped early left no bounds, no complete extraction
+            ctx->bounds.valid = false;
+            memo_invalidate(ctx);
+        }
         check_async_errors(h.err);
     };
     TC_CUDA(cudaMemsetAsync(aux, 0, 64, s));
@@ -372,6 +388,9 @@ static LoopState run_loop(tc_ctx* ctx, const tc_job* job, const float* x, int k,
     e.cal_select = cal_select;
     e.precision = job->precision;
     e.counts = nullptr;
+    e.memo = 1;  // the run's own copy of the series, fixed for the run
+    memo_invalidate(ctx);  // the copy was rewritten for this run
+    memo_prepare(ctx, e, s);  // before the extraction graph is captured
     auto issue_extract = [&]() {
         extract_async(ctx, e, s);
         TC_CUDA(cudaMemcpyAsync(aux + 16, ws.scal.p, 2 * sizeof(int32_t), cudaMemcpyDeviceToDevice, s));
@@ -412,6 +431,7 @@ static LoopState run_loop(tc_ctx* ctx, const tc_job* job, const float* x, int k,
         g_extract.run(graphs, s, issue_extract);
         readback();
         check_guards(ctx, "extraction");
+        if (h.bad_label) memo_invalidate(ctx);
         TC_REQUIRE(h.bad_label == 0, TC_ERR_ARG, "a label is outside [0, k)");
         if (!cal_select) st.sum_class = h.sum_class;  // get_class_centers_a leaves sum_class alone
     };
@@ -476,13 +496,16 @@ static std::vector<DevBuf*> workspace_buffers(tc_ctx* ctx) {
             &w.seg,  &w.perm,    &w.chunk_counts, &w.counts, &w.offsets,  &w.gate,      &w.scal,
             &w.gram, &w.rowsum,  &w.gram_yt,    &w.gram_poff, &w.piter,   &w.pstats,    &w.aux,
             &w.toeplitz, &w.toeplitz_norm, &w.xbf, &w.xbf_norm, &w.first, &w.gram_sq, &w.sq_meta, &w.screen, &w.gram_part,
-            &w.bounds, &w.cprev, &w.bstate, &w.bperm, &w.xbfp, &w.tmask};
+            &w.bounds, &w.cprev, &w.bstate, &w.bperm, &w.xbfp, &w.tmask, &w.memo_labels, &w.memo_c,
+            &w.memo_flags, &w.memo_count};
 }
 
 void release_workspace(tc_ctx* ctx) {
     for (DevBuf* b : workspace_buffers(ctx)) b->release();
     ctx->prep_x = nullptr;
     ctx->bounds.valid = false;
+    ctx->memo.keyed = false;
+    ctx->memo.counters = false;
 }
 
 size_t workspace_bytes(tc_ctx* ctx) {
@@ -629,6 +652,21 @@ int tc_assign_stats(const tc_ctx* ctx, uint64_t* screened, uint64_t* bounded, ui
     return TC_OK;
 }
 
+int tc_extract_stats(tc_ctx* ctx, uint64_t* extractions, uint64_t* clusters, uint64_t* reused) {
+    if (!ctx) return TC_ERR_ARG;
+    TC_API_BEGIN
+    uint64_t h[3] = {0, 0, 0};
+    if (ctx->memo.counters && ctx->ws.memo_count.p) {
+        TC_CUDA(cudaSetDevice(ctx->device));
+        TC_CUDA(cudaDeviceSynchronize());
+        TC_CUDA(cudaMemcpy(h, ctx->ws.memo_count.p, sizeof(h), cudaMemcpyDeviceToHost));
+    }
+    if (extractions) *extractions = h[0];
+    if (clusters) *clusters = h[1];
+    if (reused) *reused = h[2];
+    TC_API_END(ctx)
+}
+
 int tc_prepare_series(tc_ctx* ctx, const float* d_x, int64_t n, int m, tc_stream stream) {
     if (!ctx) return TC_ERR_ARG;
     TC_API_BEGIN
@@ -660,6 +698,9 @@ int tc_extract_shapes(tc_ctx* ctx, const float* d_x, const int32_t* d_labels, co
     e.cal_select = cal_select ? 1 : 0;
     e.precision = precision;
     e.counts = d_counts;
+    // prepared series are fixed until prepared again: clusters that kept their members
+    // and centroid reuse the previous extraction's output
+    e.memo = ctx->prep_x == d_x && ctx->prep_n == n && ctx->prep_m == m && !d_shift;
     int sc = run_extract(ctx, e, (cudaStream_t)stream);
     if (h_sum_class) *h_sum_class = sc;
     TC_API_END(ctx)

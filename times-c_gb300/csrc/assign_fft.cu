@@ -178,11 +178,9 @@ struct Cfg {
     static constexpr int BLOCK = T > 512 ? T : 512;
     static constexpr int TEAMS = BLOCK / T;
     static constexpr size_t BUF_BYTES = (size_t)BufSize<N>::value * sizeof(float2);
-    static constexpr int LBC = 32;  // bounded pass: bounds staged per team, a chunk of centroids at a time
-    static size_t smem(int k, bool csmem, bool bounded = false) {
+    static size_t smem(int k, bool csmem) {
         size_t s = (size_t)TEAMS * (BUF_BYTES + sizeof(TeamScratch));
         if (csmem) s += ((size_t)k * (N + 1) * sizeof(float2) + 15) / 16 * 16;  // as laid out in the kernel
-        if (bounded) s += (size_t)TEAMS * 2 * LBC * sizeof(float);
         return s;
     }
 };
@@ -229,12 +227,9 @@ struct AssignParams {
     // screened assignment: only centroids cand[i][0 .. ncand[i]) (ascending; -1: all)
     const int32_t* cand;
     const int32_t* ncand;
-    // lower bounds [k][n] on the exact distances (see launch_assign_fft)
+    // lower bounds [n][k] on the exact distances: d32 - lb_eps for every pair evaluated
     float* lb_out;
-    const float* lb_in;
-    const float* delta;
     float lb_eps;
-    unsigned long long* evals;
 };
 
 // Max NCC over the valid lags with the lag of the first maximum in sbd3D's order
@@ -264,7 +259,7 @@ struct MaxOut {
     }
 };
 
-template <int N, bool CSMEM, bool SHIFT, bool BOUNDED>
+template <int N, bool CSMEM, bool SHIFT>
 __global__ void __launch_bounds__(Cfg<N>::BLOCK, 1) k_assign_fft(AssignParams p) {
     typedef Core<N> Co;
     constexpr int T = Co::T, TEAMS = Cfg<N>::TEAMS;
@@ -275,8 +270,6 @@ __global__ void __launch_bounds__(Cfg<N>::BLOCK, 1) k_assign_fft(AssignParams p)
     const int team = threadIdx.x / T, tid = threadIdx.x % T;
     float2* buf = reinterpret_cast<float2*>(cur) + (size_t)team * BufSize<N>::value;
     TeamScratch* scr = reinterpret_cast<TeamScratch*>(cur + (size_t)TEAMS * Cfg<N>::BUF_BYTES) + team;
-    float* lbs = reinterpret_cast<float*>(cur + (size_t)TEAMS * (Cfg<N>::BUF_BYTES + sizeof(TeamScratch))) +
-                 (size_t)team * 2 * Cfg<N>::LBC;  // bounded pass: this team's bounds in, then out
 
     if (CSMEM) {
         const size_t nv = (size_t)p.k * (N + 1);
@@ -287,7 +280,6 @@ __global__ void __launch_bounds__(Cfg<N>::BLOCK, 1) k_assign_fft(AssignParams p)
     const unsigned vmask = Co::template Pass<Plan<N>::NPASS - 1>::valid_mask(tid, p.m, p.F);
     double dsum = 0.0;
     int nchg = 0;
-    unsigned long long nev = 0;
     const int64_t stride = (int64_t)gridDim.x * TEAMS;
     for (int64_t i = (int64_t)blockIdx.x * TEAMS + team; i < p.n; i += stride) {
         if (p.fixed && p.gate && !p.gate[p.fixed[i]]) {  // uniform over the team
@@ -337,79 +329,29 @@ __global__ void __launch_bounds__(Cfg<N>::BLOCK, 1) k_assign_fft(AssignParams p)
         };
         float bestd = 1e10f;  // get_pos_idx: min_val = 1e10, pos = 0
         int bestj = 0, bests = 0;
-        if constexpr (BOUNDED) {
-            // the previous label first, then every other centroid in ascending order
-            // unless its bound (carried over with the centroid's movement) shows the
-            // distance exceeds the best so far: the same first minimum as evaluating all.
-            // The bounds (series-major, p.lb_in == p.lb_out allowed) are staged through
-            // shared memory LBC centroids at a time: a chunk is read by the whole team
-            // into lbs, decided on (new bounds into a second array), and written back
-            // after a team barrier, so no thread reads a bound another has rewritten.
-            // the label the previous assignment left in the output (read by every thread
-            // before thread 0 overwrites it, past the team barriers below)
-            int j0 = p.labels[i];
-            if (j0 < 0 || j0 >= p.k) j0 = p.old_labels ? p.old_labels[i] : 0;
-            if (j0 < 0 || j0 >= p.k) j0 = 0;
-            const float d0 = distance(eval(j0));
-            bestd = d0;
-            bestj = j0;
-            int ne = 1;
-            const float* lbi = p.lb_in + (size_t)i * p.k;
-            float* lbo = p.lb_out + (size_t)i * p.k;
-            constexpr int LBC = Cfg<N>::LBC;
-            for (int c0 = 0; c0 < p.k; c0 += LBC) {
-                const int nc = min(LBC, p.k - c0);
-                for (int t = tid; t < nc; t += T) lbs[t] = __fsub_rd(__ldg(lbi + c0 + t), __ldg(p.delta + c0 + t));
-                team_sync<T>(team);
-                for (int t = 0; t < nc; ++t) {
-                    const int c = c0 + t;
-                    const float lb = lbs[t];  // the same value in every thread: decisions are uniform
-                    float nb;
-                    if (c == j0) {
-                        nb = __fsub_rd(d0, p.lb_eps);
-                    } else if (__fsub_rd(lb, p.lb_eps) > bestd) {
-                        nb = lb;
-                    } else {
-                        const float d = distance(eval(c));  // ends with a team barrier
-                        ++ne;
-                        nb = __fsub_rd(d, p.lb_eps);
-                        if (d < bestd || (d == bestd && c < bestj)) {
-                            bestd = d;
-                            bestj = c;
-                        }
-                    }
-                    if (tid == 0) lbs[LBC + t] = nb;
-                }
-                team_sync<T>(team);
-                for (int t = tid; t < nc; t += T) lbo[c0 + t] = lbs[LBC + t];
-                team_sync<T>(team);  // the next chunk overwrites lbs
-            }
-            nev += (unsigned long long)ne;
-        } else {
-            int c0 = 0, c1 = p.k;
-            if (p.fixed) {
-                c0 = p.fixed[i];
-                c1 = c0 + 1;
-            }
-            // screened: the candidates in ascending order (every centroid that can be the
-            // first minimum), so the first strict minimum below is the unscreened one
-            const int32_t* cl = nullptr;
-            int ncl = -1;
-            if (p.cand) {
-                cl = p.cand + (size_t)i * SCREEN_CAP;
-                ncl = screen_list_len(cl, p.ncand[i], p.k);
-            }
-            const int iters = ncl >= 0 ? ncl : c1 - c0;
-            for (int it = 0; it < iters; ++it) {
-                const int c = ncl >= 0 ? cl[it] : c0 + it;
-                const LagMax lm = eval(c);
-                const float d = distance(lm);
-                if (tid == 0 && p.lb_out) p.lb_out[(size_t)i * p.k + c] = __fsub_rd(d, p.lb_eps);
-                if (d < bestd) {
-                    bestd = d;
-                    bestj = c;
-                    bests = -lm.u;
-                }
+        int c0 = 0, c1 = p.k;
+        if (p.fixed) {
+            c0 = p.fixed[i];
+            c1 = c0 + 1;
+        }
+        // screened: the candidates in ascending order (every centroid that can be the
+        // first minimum), so the first strict minimum below is the unscreened one
+        const int32_t* cl = nullptr;
+        int ncl = -1;
+        if (p.cand) {
+            cl = p.cand + (size_t)i * SCREEN_CAP;
+            ncl = screen_list_len(cl, p.ncand[i], p.k);
+        }
+        const int iters = ncl >= 0 ? ncl : c1 - c0;
+        for (int it = 0; it < iters; ++it) {
+            const int c = ncl >= 0 ? cl[it] : c0 + it;
+            const LagMax lm = eval(c);
+            const float d = distance(lm);
+            if (tid == 0 && p.lb_out) p.lb_out[(size_t)i * p.k + c] = __fsub_rd(d, p.lb_eps);
+            if (d < bestd) {
+                bestd = d;
+                bestj = c;
+                bests = -lm.u;
             }
         }
         if (tid == 0) {
@@ -423,7 +365,6 @@ __global__ void __launch_bounds__(Cfg<N>::BLOCK, 1) k_assign_fft(AssignParams p)
     if (tid == 0) {
         if (p.dist_sum) atomicAdd(p.dist_sum, dsum);
         if (p.changed && nchg) atomicAdd(p.changed, nchg);
-        if (BOUNDED && p.evals && nev) atomicAdd(p.evals, nev);
     }
 }
 
@@ -445,11 +386,11 @@ struct AssignPlan {
     int blocks_per_sm;  // 0: the occupancy maximum
 };
 
-template <int N, bool CSMEM, bool SHIFT, bool BOUNDED>
+template <int N, bool CSMEM, bool SHIFT>
 static void launch_variant(tc_ctx* ctx, const AssignParams& p, int blocks_per_sm, cudaStream_t s) {
-    auto fn = k_assign_fft<N, CSMEM, SHIFT, BOUNDED>;
+    auto fn = k_assign_fft<N, CSMEM, SHIFT>;
     allow_max_dynamic_smem(fn);
-    const size_t sm = Cfg<N>::smem(p.k, CSMEM, BOUNDED);
+    const size_t sm = Cfg<N>::smem(p.k, CSMEM);
     int per_sm = 0;
     TC_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, Cfg<N>::BLOCK, sm));
     per_sm = std::max(per_sm, 1);
@@ -459,10 +400,10 @@ static void launch_variant(tc_ctx* ctx, const AssignParams& p, int blocks_per_sm
     fn<<<grid, Cfg<N>::BLOCK, sm, s>>>(p);
 }
 
-template <int N, bool SHIFT, bool BOUNDED>
+template <int N, bool SHIFT>
 static void launch_plan(tc_ctx* ctx, const AssignParams& p, const AssignPlan& pl, cudaStream_t s) {
-    if (pl.csmem) launch_variant<N, true, SHIFT, BOUNDED>(ctx, p, pl.blocks_per_sm, s);
-    else launch_variant<N, false, SHIFT, BOUNDED>(ctx, p, pl.blocks_per_sm, s);
+    if (pl.csmem) launch_variant<N, true, SHIFT>(ctx, p, pl.blocks_per_sm, s);
+    else launch_variant<N, false, SHIFT>(ctx, p, pl.blocks_per_sm, s);
 }
 
 // Autotuner: the first assignment of a shape (FFT length, k, shift output) on a
@@ -472,12 +413,11 @@ static void launch_plan(tc_ctx* ctx, const AssignParams& p, const AssignPlan& pl
 // included.  Candidates: spectra in shared memory (when they fit) or not, times
 // the occupancy maximum, half of it and one block per SM.  Off with TIMESC_AUTOTUNE=0,
 // and never inside a stream capture (the default plan is used then).
-template <int N, bool SHIFT, bool BOUNDED>
+template <int N, bool SHIFT>
 static AssignPlan tuned_plan(tc_ctx* ctx, const AssignParams& p, cudaStream_t s) {
-    const bool fits = Cfg<N>::smem(p.k, true, BOUNDED) <= ctx->smem_optin;
+    const bool fits = Cfg<N>::smem(p.k, true) <= ctx->smem_optin;
     const AssignPlan dflt{fits, 0};
-    const uint64_t key = ((uint64_t)N << 40) | ((uint64_t)p.k << 8) | (SHIFT ? 1u : 0u) | (p.cand ? 2u : 0u) |
-                         (BOUNDED ? 4u : 0u);
+    const uint64_t key = ((uint64_t)N << 40) | ((uint64_t)p.k << 8) | (SHIFT ? 1u : 0u) | (p.cand ? 2u : 0u);
     for (const auto& t : ctx->tuned)
         if (t.first == key) return AssignPlan{(t.second & 1u) != 0, (int)(t.second >> 1)};
     const char* env = std::getenv("TIMESC_AUTOTUNE");
@@ -490,7 +430,6 @@ static AssignPlan tuned_plan(tc_ctx* ctx, const AssignParams& p, cudaStream_t s)
     q.n = sample;
     q.changed = nullptr;
     q.dist_sum = nullptr;
-    q.evals = nullptr;
     std::vector<AssignPlan> cands;
     for (int cs = fits ? 1 : 0; cs >= 0; --cs)
         for (int b : {0, -2, 1}) cands.push_back(AssignPlan{cs != 0, b});
@@ -504,18 +443,16 @@ static AssignPlan tuned_plan(tc_ctx* ctx, const AssignParams& p, cudaStream_t s)
             int per_sm = 0;
             if (c.csmem)
                 TC_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-                    &per_sm, k_assign_fft<N, true, SHIFT, BOUNDED>, Cfg<N>::BLOCK,
-                    Cfg<N>::smem(p.k, true, BOUNDED)));
+                    &per_sm, k_assign_fft<N, true, SHIFT>, Cfg<N>::BLOCK, Cfg<N>::smem(p.k, true)));
             else
                 TC_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-                    &per_sm, k_assign_fft<N, false, SHIFT, BOUNDED>, Cfg<N>::BLOCK,
-                    Cfg<N>::smem(p.k, false, BOUNDED)));
+                    &per_sm, k_assign_fft<N, false, SHIFT>, Cfg<N>::BLOCK, Cfg<N>::smem(p.k, false)));
             if (per_sm < 2) continue;
             c.blocks_per_sm = per_sm / 2;
         }
-        launch_plan<N, SHIFT, BOUNDED>(ctx, q, c, s);  // warm
+        launch_plan<N, SHIFT>(ctx, q, c, s);  // warm
         TC_CUDA(cudaEventRecord(e0, s));
-        for (int r = 0; r < 2; ++r) launch_plan<N, SHIFT, BOUNDED>(ctx, q, c, s);
+        for (int r = 0; r < 2; ++r) launch_plan<N, SHIFT>(ctx, q, c, s);
         TC_CUDA(cudaEventRecord(e1, s));
         TC_CUDA(cudaEventSynchronize(e1));
         TC_CUDA(cudaGetLastError());
@@ -530,9 +467,8 @@ static AssignPlan tuned_plan(tc_ctx* ctx, const AssignParams& p, cudaStream_t s)
     cudaEventDestroy(e1);
     ctx->tuned.emplace_back(key, (uint32_t)(pick.csmem ? 1 : 0) | ((uint32_t)pick.blocks_per_sm << 1));
     if (std::getenv("TIMESC_TRACE"))
-        std::fprintf(stderr, "timesc: autotune assignment F=%d k=%d shift=%d bounded=%d -> spectra %s, %d blocks/SM\n",
-                     2 * N, p.k, (int)SHIFT, (int)BOUNDED, pick.csmem ? "in shared memory" : "through L1",
-                     pick.blocks_per_sm);
+        std::fprintf(stderr, "timesc: autotune assignment F=%d k=%d shift=%d -> spectra %s, %d blocks/SM\n", 2 * N,
+                     p.k, (int)SHIFT, pick.csmem ? "in shared memory" : "through L1", pick.blocks_per_sm);
     return pick;
 }
 
@@ -560,24 +496,10 @@ static void assign_n(tc_ctx* ctx, const AssignArgs& a, cudaStream_t s) {
     p.cand = a.cand;
     p.ncand = a.ncand;
     p.lb_out = a.lb_out;
-    p.lb_in = a.lb_in;
-    p.delta = a.delta;
     p.lb_eps = a.lb_eps;
-    p.evals = a.evals;
     const bool want_shift = a.shift != nullptr || a.fixed != nullptr;
-    if (a.lb_in) {
-        // the bounded pass exists where its bounds come from: the screened lengths (F 128..1024)
-        if constexpr (N >= 64 && N <= 512) {
-            TC_REQUIRE(!want_shift && a.lb_out && a.delta, TC_ERR_ARG, "bounded assignment: arguments");
-            launch_plan<N, false, true>(ctx, p, tuned_plan<N, false, true>(ctx, p, s), s);
-        } else {
-            throw TcError{TC_ERR_UNSUPPORTED, "bounded assignment: FFT length outside 128..1024"};
-        }
-    } else if (want_shift) {
-        launch_plan<N, true, false>(ctx, p, tuned_plan<N, true, false>(ctx, p, s), s);
-    } else {
-        launch_plan<N, false, false>(ctx, p, tuned_plan<N, false, false>(ctx, p, s), s);
-    }
+    if (want_shift) launch_plan<N, true>(ctx, p, tuned_plan<N, true>(ctx, p, s), s);
+    else launch_plan<N, false>(ctx, p, tuned_plan<N, false>(ctx, p, s), s);
     TC_CHECK_LAUNCH();
 }
 
@@ -750,7 +672,7 @@ static void noalloc_n(const NoallocDevice& d, const float* x, const float* C, in
     p.dist = dist;
     const bool csmem = Cfg<N>::smem(k, true) <= d.smem_optin;
     const size_t sm = Cfg<N>::smem(k, csmem);
-    auto fn = csmem ? k_assign_fft<N, true, false, false> : k_assign_fft<N, false, false, false>;
+    auto fn = csmem ? k_assign_fft<N, true, false> : k_assign_fft<N, false, false>;
     allow_max_dynamic_smem(fn);
     int per_sm = 0;
     TC_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, Cfg<N>::BLOCK, sm));

@@ -169,6 +169,8 @@ struct AtParams {
     // centroid, and that centroid (the bounded BF16 pass reads and rewrites them)
     float* ubd;
     int32_t* jb;
+    // full pass before a grouping: per series best * k + second best (the group key)
+    int32_t* gkey;
     // tile-bounded pass: the tiles hold cluster-grouped positions (perm maps a position
     // to its series, for the outputs and bounds); only the centroids of tmask[tile]
     // are evaluated, and the other bounds of the tile's series are carried down by
@@ -354,6 +356,8 @@ __global__ void __launch_bounds__(AT_THREADS, 1) k_assign_tc(const __grid_consta
                 atomicAdd(p.evals, (unsigned long long)__popcll((long long)tmask));
             float bestd = 1e10f;  // get_pos_idx: min_val = 1e10, pos = 0
             int bestj = 0;
+            float secd = 1e10f;  // the second best (group key of a full pass)
+            int secj = 0;
             int cj[SCREEN_CAP];
             float cd[SCREEN_CAP];
 #pragma unroll
@@ -399,8 +403,13 @@ __global__ void __launch_bounds__(AT_THREADS, 1) k_assign_tc(const __grid_consta
                 if (p.clamp2 && d > 2.0f) d = 2.0f;
                 if (p.lb_out && pos < p.n) p.lb_out[(size_t)i * p.k + j] = __fsub_rd(d, p.lb_d16);
                 if (d < bestd) {
+                    secd = bestd;
+                    secj = bestj;
                     bestd = d;
                     bestj = j;
+                } else if (d < secd) {
+                    secd = d;
+                    secj = j;
                 }
                 if (p.cand && nc >= 0 && !(d > bestd + p.thr)) {
                     if (nc == SCREEN_CAP) nc = screen_compact(cj, cd, nc, bestd + p.thr);
@@ -430,6 +439,7 @@ __global__ void __launch_bounds__(AT_THREADS, 1) k_assign_tc(const __grid_consta
                     p.ubd[i] = __fadd_ru(bestd, p.lb_d16);
                     p.jb[i] = bestj;
                 }
+                if (p.gkey) p.gkey[i] = bestj * p.k + secj;
                 if (p.cand) {
                     if (nc >= 0) nc = screen_compact(cj, cd, nc, bestd + p.thr);
                     int4* o = reinterpret_cast<int4*>(p.cand + (size_t)i * SCREEN_CAP);
@@ -468,44 +478,60 @@ __global__ void __launch_bounds__(AT_THREADS, 1) k_assign_tc(const __grid_consta
 // a stored best centroid, kept inside [0, k) whatever the buffer holds
 __device__ __forceinline__ int group_of(int j, int k) { return (j >= 0 && j < k) ? j : 0; }
 
-// per-label counts: block histogram in shared memory, one global add per label
-__global__ void k_group_count(const int32_t* __restrict__ jb, int64_t n, int k, int32_t* __restrict__ cnt) {
+// per-key counts: block histogram in shared memory, one global add per key
+__global__ void k_group_count(const int32_t* __restrict__ key, int64_t n, int nb, int32_t* __restrict__ cnt) {
     extern __shared__ int32_t hist[];
-    for (int j = threadIdx.x; j < k; j += blockDim.x) hist[j] = 0;
+    for (int j = threadIdx.x; j < nb; j += blockDim.x) hist[j] = 0;
     __syncthreads();
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < n) atomicAdd(&hist[group_of(jb[i], k)], 1);
+    if (i < n) atomicAdd(&hist[group_of(key[i], nb)], 1);
     __syncthreads();
-    for (int j = threadIdx.x; j < k; j += blockDim.x)
+    for (int j = threadIdx.x; j < nb; j += blockDim.x)
         if (hist[j]) atomicAdd(&cnt[j], hist[j]);
 }
 
-// cursor[j] = start of group j (exclusive scan of the counts)
-__global__ void k_group_offsets(const int32_t* __restrict__ cnt, int k, int32_t* __restrict__ cursor) {
-    int acc = 0;
-    for (int j = 0; j < k; ++j) {
-        cursor[j] = acc;
-        acc += cnt[j];
+// cursor[j] = start of group j (exclusive scan of the counts; one block, chunks of
+// 1024 keys scanned in shared memory)
+__global__ void __launch_bounds__(1024) k_group_offsets(const int32_t* __restrict__ cnt, int nb,
+                                                        int32_t* __restrict__ cursor) {
+    __shared__ int32_t buf[1024];
+    __shared__ int32_t carry;
+    if (threadIdx.x == 0) carry = 0;
+    for (int b0 = 0; b0 < nb; b0 += 1024) {
+        const int j = b0 + threadIdx.x;
+        const int v = j < nb ? cnt[j] : 0;
+        buf[threadIdx.x] = v;
+        __syncthreads();
+        for (int o = 1; o < 1024; o <<= 1) {  // inclusive Hillis-Steele scan
+            const int add = threadIdx.x >= o ? buf[threadIdx.x - o] : 0;
+            __syncthreads();
+            buf[threadIdx.x] += add;
+            __syncthreads();
+        }
+        if (j < nb) cursor[j] = carry + buf[threadIdx.x] - v;
+        __syncthreads();
+        if (threadIdx.x == 0) carry += buf[1023];
+        __syncthreads();
     }
 }
 
-// perm[position] = series: each block reserves a range per label, then places its series
-__global__ void k_group_scatter(const int32_t* __restrict__ jb, int64_t n, int k, int32_t* __restrict__ cursor,
+// perm[position] = series: each block reserves a range per key, then places its series
+__global__ void k_group_scatter(const int32_t* __restrict__ key, int64_t n, int nb, int32_t* __restrict__ cursor,
                                 int32_t* __restrict__ perm) {
-    extern __shared__ int32_t hist[];  // [k] counts, then [k] reserved starts
-    for (int j = threadIdx.x; j < 2 * k; j += blockDim.x) hist[j] = 0;
+    extern __shared__ int32_t hist[];  // [nb] counts, then [nb] reserved starts
+    for (int j = threadIdx.x; j < 2 * nb; j += blockDim.x) hist[j] = 0;
     __syncthreads();
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     int lab = 0, rank = 0;
     if (i < n) {
-        lab = group_of(jb[i], k);
+        lab = group_of(key[i], nb);
         rank = atomicAdd(&hist[lab], 1);
     }
     __syncthreads();
-    for (int j = threadIdx.x; j < k; j += blockDim.x)
-        if (hist[j]) hist[k + j] = atomicAdd(&cursor[j], hist[j]);
+    for (int j = threadIdx.x; j < nb; j += blockDim.x)
+        if (hist[j]) hist[nb + j] = atomicAdd(&cursor[j], hist[j]);
     __syncthreads();
-    if (i < n) perm[hist[k + lab] + rank] = (int32_t)i;
+    if (i < n) perm[hist[nb + lab] + rank] = (int32_t)i;
 }
 
 // the BF16 rows and norms in position order (one warp per row, 16-byte copies)
@@ -539,9 +565,28 @@ __global__ void __launch_bounds__(128) k_tile_masks(const int32_t* __restrict__ 
         const float ub = __fadd_ru(__fadd_ru(ubd[i], __ldg(delta + j0)), D);
         mask = 1ull << j0;
         const float* lr = lb + (size_t)i * k;
-        for (int j = 0; j < k; ++j) {
-            const float l = __fsub_rd(__fsub_rd(lr[j], __ldg(delta + j)), D);
+        auto test = [&](int j, float b) {
+            const float l = __fsub_rd(__fsub_rd(b, __ldg(delta + j)), D);
             if (!(l > ub)) mask |= 1ull << j;
+        };
+        if ((k & 3) == 0) {  // the row as float4s, all loads issued before the tests (rows are 16-byte aligned)
+            const float4* l4 = reinterpret_cast<const float4*>(lr);
+            for (int j = 0; j < k; j += 32) {
+                float4 v[8];
+#pragma unroll
+                for (int q = 0; q < 8; ++q)
+                    if (j + 4 * q < k) v[q] = __ldg(l4 + j / 4 + q);
+#pragma unroll
+                for (int q = 0; q < 8; ++q)
+                    if (j + 4 * q < k) {
+                        test(j + 4 * q, v[q].x);
+                        test(j + 4 * q + 1, v[q].y);
+                        test(j + 4 * q + 2, v[q].z);
+                        test(j + 4 * q + 3, v[q].w);
+                    }
+            }
+        } else {
+            for (int j = 0; j < k; ++j) test(j, lr[j]);
         }
     }
     const unsigned lo = __reduce_or_sync(0xffffffffu, (unsigned)mask);
@@ -551,36 +596,51 @@ __global__ void __launch_bounds__(128) k_tile_masks(const int32_t* __restrict__ 
     if (threadIdx.x == 0) tmask[blockIdx.x] = part[0] | part[1] | part[2] | part[3];
 }
 
-void launch_tile_bounds(tc_ctx* ctx, int64_t n, int m, int k, const float* lb, const float* ubd, const int32_t* jb,
-                        const float* delta, float D, TileBounds& out, cudaStream_t s) {
+// The grouped layout in the workspace: positions -> series, and the BF16 rows and
+// norms in position order.
+static TileBounds tile_layout(tc_ctx* ctx, int64_t n, int m, int k) {
     Workspace& ws = ctx->ws;
     const int mp = (m + 63) / 64 * 64;
-    const int64_t ntiles = (n + AT_TILE - 1) / AT_TILE;
-    int32_t* perm = ws.bperm.as<int32_t>((size_t)n + 2 * k);
-    int32_t* cnt = perm + n;
-    int32_t* cursor = cnt + k;
+    TileBounds t;
+    t.perm = ws.bperm.as<int32_t>((size_t)n + 2 * (size_t)k * k);  // + group counts and cursors
     char* xp = static_cast<char*>(ws.xbfp.get((size_t)n * mp * 2 + (size_t)n * 4 + 16));
-    __nv_bfloat16* xbp = reinterpret_cast<__nv_bfloat16*>(xp);
-    float* normp = reinterpret_cast<float*>(xp + (size_t)n * mp * 2);
-    unsigned long long* tmask = ws.tmask.as<unsigned long long>((size_t)ntiles);
+    t.xbf = xp;
+    t.xbf_norm = reinterpret_cast<const float*>(xp + (size_t)n * mp * 2);
+    t.tmask = ws.tmask.as<unsigned long long>((size_t)((n + AT_TILE - 1) / AT_TILE));
+    return t;
+}
+
+void launch_tile_group(tc_ctx* ctx, int64_t n, int m, int k, const int32_t* gkey, cudaStream_t s) {
+    Workspace& ws = ctx->ws;
+    const int mp = (m + 63) / 64 * 64;
+    const TileBounds t = tile_layout(ctx, n, m, k);
+    const int nb = k * k;  // groups: (best, second best)
+    int32_t* perm = const_cast<int32_t*>(t.perm);
+    int32_t* cnt = perm + n;
+    int32_t* cursor = cnt + nb;
+    __nv_bfloat16* xbp = static_cast<__nv_bfloat16*>(const_cast<void*>(t.xbf));
+    float* normp = const_cast<float*>(t.xbf_norm);
     const __nv_bfloat16* xb = ws.xbf.as<__nv_bfloat16>((size_t)n * mp);
     const float* xnorm = ws.xbf_norm.as<float>((size_t)n);
-    TC_CUDA(cudaMemsetAsync(cnt, 0, sizeof(int32_t) * k, s));
+    TC_CUDA(cudaMemsetAsync(cnt, 0, sizeof(int32_t) * nb, s));
     const int gb = ceil_div(n, 1024);
-    k_group_count<<<gb, 1024, sizeof(int32_t) * k, s>>>(jb, n, k, cnt);
+    k_group_count<<<gb, 1024, sizeof(int32_t) * nb, s>>>(gkey, n, nb, cnt);
     TC_CHECK_LAUNCH();
-    k_group_offsets<<<1, 1, 0, s>>>(cnt, k, cursor);
+    k_group_offsets<<<1, 1024, 0, s>>>(cnt, nb, cursor);
     TC_CHECK_LAUNCH();
-    k_group_scatter<<<gb, 1024, sizeof(int32_t) * 2 * k, s>>>(jb, n, k, cursor, perm);
+    k_group_scatter<<<gb, 1024, sizeof(int32_t) * 2 * nb, s>>>(gkey, n, nb, cursor, perm);
     TC_CHECK_LAUNCH();
     k_permute_bf16<<<ceil_div(n * 32, 256), 256, 0, s>>>(xb, xnorm, perm, n, mp, xbp, normp);
     TC_CHECK_LAUNCH();
-    k_tile_masks<<<(unsigned)ntiles, 128, 0, s>>>(perm, lb, ubd, jb, delta, D, n, k, tmask);
+}
+
+void launch_tile_masks(tc_ctx* ctx, int64_t n, int m, int k, const float* lb, const float* ubd, const int32_t* jb,
+                       const float* delta, float D, TileBounds& out, cudaStream_t s) {
+    out = tile_layout(ctx, n, m, k);
+    const int64_t ntiles = (n + AT_TILE - 1) / AT_TILE;
+    k_tile_masks<<<(unsigned)ntiles, 128, 0, s>>>(out.perm, lb, ubd, jb, delta, D, n, k,
+                                                  const_cast<unsigned long long*>(out.tmask));
     TC_CHECK_LAUNCH();
-    out.perm = perm;
-    out.xbf = xbp;
-    out.xbf_norm = normp;
-    out.tmask = tmask;
 }
 
 // ---------------------------------------------------------------- host
@@ -611,6 +671,7 @@ void prepare_series_bf16_done(tc_ctx* ctx, const float* x, int64_t n, int m) {
     ctx->prep_n = n;
     ctx->prep_m = m;
     ctx->bounds.valid = false;  // new series contents: bounds on old distances no longer hold
+    memo_invalidate(ctx);       // and the extraction memo's outputs neither
 }
 
 void prepare_series_bf16(tc_ctx* ctx, const float* x, int64_t n, int m, cudaStream_t s) {
@@ -701,6 +762,7 @@ void launch_assign_tc(tc_ctx* ctx, const AssignArgs& a, int precision, cudaStrea
     p.lb_d16 = a.lb_d16;
     p.ubd = a.ubd;
     p.jb = a.jb;
+    p.gkey = a.gkey;
     p.tmask = a.tmask;
     p.perm = a.perm;
     p.delta = a.delta;

@@ -177,12 +177,12 @@ __global__ void k_gate(const float* __restrict__ C, int m, int mode, uint8_t* __
 // 32-row slabs; FP32 sums of 256 rows are folded into a compensated total.
 __global__ void __launch_bounds__(256) k_gram_simt(const float* __restrict__ Y, const int32_t* __restrict__ counts,
                                                    const int32_t* __restrict__ offsets, int m, int ld, int nt,
-                                                   float* __restrict__ S) {
+                                                   float* __restrict__ S, const uint8_t* __restrict__ skip) {
     __shared__ __align__(16) float As[32][64];
     __shared__ __align__(16) float Bs[32][64];
     const int c = blockIdx.y;
     const int cnt = counts[c];
-    if (cnt == 0) return;
+    if (cnt == 0 || (skip && skip[c])) return;
     int t = blockIdx.x, ta = 0;
     while (t >= nt - ta) { t -= nt - ta; ++ta; }
     const int tb = ta + t;
@@ -277,9 +277,132 @@ __global__ void k_rowsum_total(const double* __restrict__ r, const int32_t* __re
     if (threadIdx.x == 0) tot[c] = s;
 }
 
+// ---------------------------------------------------------------- memo of unchanged clusters
+// Every stage of the extraction is deterministic per cluster: a centroid depends
+// only on the cluster's members (the set, taken in series order by the stable
+// segment), their alignment shifts (computed against the centroid given) and that
+// centroid.  So on the same series, a cluster whose members and input centroid equal
+// those of the previous extraction gets that extraction's output again, bit for bit:
+// its shifts, gather, Gram and power iteration are left out and the output is copied.
+// The previous extraction's labels and its input and output centroids stay in the
+// workspace, and the comparison runs on the device, so a replayed CUDA graph of the
+// extraction keeps working.  Once the loop settles, most clusters keep their members
+// from one iteration to the next.
+
+// dirty[c] = 1 where a series entered or left cluster c since the previous extraction
+__global__ void k_memo_dirty(const int32_t* __restrict__ L, const int32_t* __restrict__ Lm, int64_t n, int k,
+                             uint8_t* __restrict__ dirty) {
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const int a = L[i], b = Lm[i];
+        if (a != b) {  // every writer stores 1
+            if ((unsigned)a < (unsigned)k) dirty[a] = 1;
+            if ((unsigned)b < (unsigned)k) dirty[b] = 1;
+        }
+    }
+}
+
+// One block per cluster: skip[c] when the previous extraction is complete, c kept its
+// members and its input centroid is bitwise the previous one; the shift pass's gate
+// closes for skipped clusters.  The input centroids are kept in cin_now.
+__global__ void k_memo_skip(const float* __restrict__ C, float* __restrict__ cin_now,
+                            const float* __restrict__ cin_prev, int m, const uint8_t* __restrict__ dirty,
+                            const int* __restrict__ valid, const uint8_t* __restrict__ gate,
+                            uint8_t* __restrict__ skip, uint8_t* __restrict__ gate_shift,
+                            unsigned long long* __restrict__ count) {
+    const int c = blockIdx.x;
+    const uint32_t* a = reinterpret_cast<const uint32_t*>(C) + (size_t)c * m;
+    const uint32_t* b = reinterpret_cast<const uint32_t*>(cin_prev) + (size_t)c * m;
+    bool same = true;
+    for (int t = threadIdx.x; t < m; t += blockDim.x) {
+        const uint32_t v = a[t];
+        cin_now[(size_t)c * m + t] = __uint_as_float(v);
+        same = same && v == b[t];
+    }
+    same = __syncthreads_and(same) != 0;
+    if (threadIdx.x == 0) {
+        const bool sk = *valid != 0 && !dirty[c] && same;
+        skip[c] = sk;
+        gate_shift[c] = gate[c] && !sk;
+        if (c == 0) atomicAdd(count, 1ull);
+        atomicAdd(count + 1, 1ull);
+        if (sk) atomicAdd(count + 2, 1ull);
+    }
+}
+
+// After the extraction: skipped clusters get the previous output; the memo takes
+// this extraction's input and output centroids and is marked complete (the labels
+// are copied after this kernel).
+__global__ void k_memo_finish(float* __restrict__ C, float* __restrict__ cout_prev, float* __restrict__ cin_prev,
+                              const float* __restrict__ cin_now, const uint8_t* __restrict__ skip, int m,
+                              int* __restrict__ valid) {
+    const int c = blockIdx.x;
+    const bool sk = skip[c] != 0;
+    for (int t = threadIdx.x; t < m; t += blockDim.x) {
+        const size_t e = (size_t)c * m + t;
+        if (sk) C[e] = cout_prev[e];
+        else cout_prev[e] = C[e];
+        cin_prev[e] = cin_now[e];
+    }
+    if (c == 0 && threadIdx.x == 0) *valid = 1;
+}
+
+struct MemoBuffers {
+    int32_t* labels;
+    float *cin_prev, *cout_prev, *cin_now;
+    uint8_t *dirty, *skip, *gate_shift;
+    int* valid;
+    unsigned long long* count;
+};
+
+static MemoBuffers memo_buffers(tc_ctx* ctx, int64_t n, int k, int m) {
+    Workspace& ws = ctx->ws;
+    MemoBuffers b;
+    b.labels = ws.memo_labels.as<int32_t>(std::max<int64_t>(n, 1));
+    float* c = ws.memo_c.as<float>((size_t)3 * k * m);
+    b.cin_prev = c;
+    b.cout_prev = c + (size_t)k * m;
+    b.cin_now = c + (size_t)2 * k * m;
+    const size_t fb = ((size_t)3 * k + 15) / 16 * 16;
+    uint8_t* f = ws.memo_flags.as<uint8_t>(fb + 16);
+    b.dirty = f;
+    b.skip = f + k;
+    b.gate_shift = f + 2 * k;
+    b.valid = reinterpret_cast<int*>(f + fb);
+    if (!ctx->memo.counters || !ws.memo_count.p) {  // outside graph capture (memo_prepare comes first)
+        b.count = ws.memo_count.as<unsigned long long>(3);
+        TC_CUDA(cudaMemset(b.count, 0, 3 * sizeof(unsigned long long)));
+        ctx->memo.counters = true;
+    }
+    b.count = static_cast<unsigned long long*>(ws.memo_count.p);
+    return b;
+}
+
+static bool memo_keyed_for(const tc_ctx* ctx, const ExtractArgs& a) {
+    const MemoState& ms = ctx->memo;
+    return ms.keyed && ms.x == a.x && ms.n == a.n && ms.m == a.m && ms.k == a.k && ms.mode == a.mode &&
+           ms.precision == a.precision && ms.cal_select == a.cal_select;
+}
+
+void memo_prepare(tc_ctx* ctx, const ExtractArgs& a, cudaStream_t s) {
+    if (!a.memo || a.n <= 0) return;
+    const MemoBuffers b = memo_buffers(ctx, a.n, a.k, a.m);  // allocated here, before any capture
+    if (memo_keyed_for(ctx, a)) return;
+    MemoState& ms = ctx->memo;
+    TC_CUDA(cudaMemsetAsync(b.valid, 0, sizeof(int), s));
+    ms.x = a.x;
+    ms.n = a.n;
+    ms.m = a.m;
+    ms.k = a.k;
+    ms.mode = a.mode;
+    ms.precision = a.precision;
+    ms.cal_select = a.cal_select;
+    ms.keyed = true;
+}
+
 void power_eigvecs(tc_ctx* ctx, const float* S, int ld, const double* r, const double* tot, const int32_t* counts,
                    const int32_t* offsets, const float* seg, bool lead_rows, int k, int m, int mode, int tmax,
-                   double tol, const float* vinit, const int32_t* vok, int tmax_sq, float* C, cudaStream_t s);
+                   double tol, const float* vinit, const int32_t* vok, int tmax_sq, float* C, cudaStream_t s,
+                   const uint8_t* skip);
 
 // ---------------------------------------------------------------- driver
 // Everything on the stream, with no host synchronisation (capturable in a CUDA
@@ -327,6 +450,28 @@ void extract_async(tc_ctx* ctx, const ExtractArgs& a, cudaStream_t s) {
     k_gate<<<k, 256, 0, s>>>(a.C, m, a.mode, gate);
     TC_CHECK_LAUNCH();
 
+    // memo of unchanged clusters: only on fixed series without caller shifts, and not
+    // with the repeated squaring (its launches cover all clusters together)
+    const bool squaring =
+        (a.cal_select || a.mode == TC_MODE_CANONICAL) && power_squaring_supported(m, k, ctx->sm_count);
+    const bool memo = a.memo && !a.shift && !squaring && n > 0 && !std::getenv("TIMESC_NO_MEMO") &&
+                      memo_keyed_for(ctx, a);  // memo_prepare sized and keyed it
+    MemoBuffers mb{};
+    const uint8_t* skip = nullptr;
+    const uint8_t* gate_shift = gate;
+    if (memo) {
+        mb = memo_buffers(ctx, n, k, m);
+        TC_CUDA(cudaMemsetAsync(mb.dirty, 0, k, s));
+        const int g = (int)std::min<int64_t>(ceil_div(n, 256), (int64_t)ctx->sm_count * 8);
+        k_memo_dirty<<<g, 256, 0, s>>>(a.labels, mb.labels, n, k, mb.dirty);
+        TC_CHECK_LAUNCH();
+        k_memo_skip<<<k, 128, 0, s>>>(a.C, mb.cin_now, mb.cin_prev, m, mb.dirty, mb.valid, gate, mb.skip,
+                                      mb.gate_shift, mb.count);
+        TC_CHECK_LAUNCH();
+        skip = mb.skip;
+        gate_shift = mb.gate_shift;
+    }
+
     const int32_t* shift = a.shift;
     if (!shift && n > 0) {
         // alignment shifts of each series against its own centroid (sbd3D, SBD.cuh:69-85)
@@ -343,7 +488,7 @@ void extract_async(tc_ctx* ctx, const ExtractArgs& a, cudaStream_t s) {
         aa.F = F;
         aa.clamp2 = 0;
         aa.fixed = a.labels;
-        aa.gate = gate;
+        aa.gate = gate_shift;  // skipped clusters need no shifts
         aa.shift = sh;
         launch_assign_fft(ctx, aa, s);
         shift = sh;
@@ -352,20 +497,19 @@ void extract_async(tc_ctx* ctx, const ExtractArgs& a, cudaStream_t s) {
     // operand when it is used (m <= 1024), else into the row-major segment buffer
     const bool tc_gram = gram_tc_supported(m, a.precision);
     const bool fused = tc_gram && gather_transposed_supported(m);
-    const bool squaring =
-        (a.cal_select || a.mode == TC_MODE_CANONICAL) && power_squaring_supported(m, k, ctx->sm_count);
     if (tc_gram && squaring)  // one operand buffer for both uses, sized before either is written
         ws.gram_yt.get(std::max(gram_operand_bytes(n, k, m, a.precision), power_squaring_operand_bytes(k, m)));
     const float* lead = nullptr;
     if (fused) {
         const GramOperand op = gram_tc_operand(ctx, n, k, m, a.precision);
         float* first = ws.first.as<float>((size_t)k * m);
-        launch_gather_norm_t(a.x, perm, a.labels, shift, gate, offsets, counts, k, poff, n, m, op.fmt == 1, op.YT,
-                             op.YTlo, op.Pp, first, s);
+        launch_gather_norm_t(a.x, perm, a.labels, shift, gate_shift, offsets, counts, k, poff, n, m, op.fmt == 1,
+                             op.YT, op.YTlo, op.Pp, first, s, skip);
         lead = first;
     } else {
         seg = ws.seg.as<float>((size_t)std::max<int64_t>(n, 1) * m);
-        launch_gather_norm(a.x, perm, a.labels, shift, gate, n, m, seg, ctx->sm_count, s);
+        // skipped clusters' rows are gathered unaligned (their shifts were not computed) and not used
+        launch_gather_norm(a.x, perm, a.labels, shift, gate_shift, n, m, seg, ctx->sm_count, s);
         lead = seg;
     }
 
@@ -374,10 +518,11 @@ void extract_async(tc_ctx* ctx, const ExtractArgs& a, cudaStream_t s) {
     TC_CUDA(cudaMemsetAsync(gram_err, 0, sizeof(int), s));
     const int nt = ceil_div(m, 64);
     if (tc_gram) {
-        launch_gram_tc(ctx, fused ? nullptr : seg, counts, offsets, poff, n, k, m, ld, a.precision, S, gram_err, s);
+        launch_gram_tc(ctx, fused ? nullptr : seg, counts, offsets, poff, n, k, m, ld, a.precision, S, gram_err, s,
+                       skip);
     } else {
         dim3 g(nt * (nt + 1) / 2, k);
-        k_gram_simt<<<g, 256, 0, s>>>(seg, counts, offsets, m, ld, nt, S);
+        k_gram_simt<<<g, 256, 0, s>>>(seg, counts, offsets, m, ld, nt, S, skip);
         TC_CHECK_LAUNCH();
     }
     k_rowsum<<<dim3(ceil_div(m, 8), k), 256, 0, s>>>(S, counts, m, ld, rs, tot);
@@ -407,16 +552,23 @@ void extract_async(tc_ctx* ctx, const ExtractArgs& a, cudaStream_t s) {
         sq = power_squaring(ctx, S, ld, rs, tot, counts, k, m, e, gram_err, s);
     }
     power_eigvecs(ctx, S, ld, rs, tot, counts, offsets, lead, fused, k, m, a.mode, tmax, tol, sq.vec, sq.ok, tmax_sq,
-                  a.C, s);
+                  a.C, s, skip);
+    if (memo) {
+        k_memo_finish<<<k, 128, 0, s>>>(a.C, mb.cout_prev, mb.cin_prev, mb.cin_now, mb.skip, m, mb.valid);
+        TC_CHECK_LAUNCH();
+        TC_CUDA(cudaMemcpyAsync(mb.labels, a.labels, sizeof(int32_t) * n, cudaMemcpyDeviceToDevice, s));
+    }
 }
 
 int run_extract(tc_ctx* ctx, const ExtractArgs& a, cudaStream_t s) {
+    memo_prepare(ctx, a, s);
     extract_async(ctx, a, s);
     int32_t h_sc[2] = {0, 0};
     int h_err = 0;
     TC_CUDA(cudaMemcpyAsync(h_sc, ctx->ws.scal.p, sizeof(int32_t) * 2, cudaMemcpyDeviceToHost, s));
     TC_CUDA(cudaMemcpyAsync(&h_err, static_cast<char*>(ctx->ws.aux.p) + 48, sizeof(int), cudaMemcpyDeviceToHost, s));
     TC_CUDA(cudaStreamSynchronize(s));
+    if (h_sc[1] || h_err) memo_invalidate(ctx);  // this extraction's outputs are not complete
     TC_REQUIRE(h_sc[1] == 0, TC_ERR_ARG, "a label is outside [0, k)");
     TC_REQUIRE(h_err == 0, TC_ERR_TIMEOUT, "tensor-core Gram: a pipeline wait ran out");
     return h_sc[0];

@@ -55,6 +55,7 @@ struct PowerClusterParams {
     const float* vinit;
     const int32_t* vok;
     int tmax_sq;
+    const uint8_t* skip;  // clusters whose centroid is kept (may be null)
 };
 
 // (s, c) += (s2, c2) where a pair means s - c; the two leading parts are added
@@ -86,7 +87,7 @@ __global__ void __launch_bounds__(PC_THREADS, 1) k_power_cluster(PowerClusterPar
     const int m = p.m, ld = p.ld;
     const int rank = (int)cluster.block_rank();
     const int c = blockIdx.x / CL;
-    if (p.counts[c] == 0) return;  // every CTA of this cluster leaves together
+    if (p.counts[c] == 0 || (p.skip && p.skip[c])) return;  // every CTA of this cluster leaves together
     const int a0 = (int)((int64_t)rank * m / CL), a1 = (int)((int64_t)(rank + 1) * m / CL);
     const int nrow = a1 - a0;
     // shared memory: v[ld] | y[2][ld] | part[2][CL][warps][4] float pairs | vprev[nrow] | r_own[nrow]
@@ -434,11 +435,12 @@ static size_t cluster_smem(int m, int ld, bool res) {
 
 void power_eigvecs(tc_ctx* ctx, const float* S, int ld, const double* r, const double* tot, const int32_t* counts,
                    const int32_t* offsets, const float* seg, bool lead_rows, int k, int m, int mode, int tmax,
-                   double tol, const float* vinit, const int32_t* vok, int tmax_sq, float* C, cudaStream_t s) {
+                   double tol, const float* vinit, const int32_t* vok, int tmax_sq, float* C, cudaStream_t s,
+                   const uint8_t* skip) {
     int* steps = ctx->ws.pstats.as<int>((size_t)k);
     const double tail = 3e-8;  // movement still to come, L2 norm of a unit vector
     PowerClusterParams pp{S,     ld,          r,     tot,   counts, offsets, seg,  lead_rows ? 1 : 0, C, k, m, tmax,
-                          mode,  tol * tol,   tail * tail,  steps,  vinit,   vok,  tmax_sq};
+                          mode,  tol * tol,   tail * tail,  steps,  vinit,   vok,  tmax_sq, skip};
     // long series stream tens of MB per step from HBM: spread each over 16 SMs
     if (m > 1024) {
         const size_t smem = cluster_smem<16>(m, ld, false);

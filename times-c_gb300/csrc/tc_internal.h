@@ -142,10 +142,25 @@ struct Workspace {
     DevBuf screen;       // n x SCREEN_CAP candidate centroids + n counts (screened FP32 assignment)
     DevBuf bounds;       // n x k f32: distance lower bounds (bounded assignment)
     DevBuf cprev;        // k x m f32 unit centroids the bounds refer to, + k f32 movements
-    DevBuf bstate;       // n f32 + n i32: per series the best centroid's upper bound and index (BF16 bounds)
+    DevBuf bstate;       // n f32 + 2n i32: per series the best centroid's upper bound and index, and group key
     DevBuf bperm;        // n i32 positions -> series, + 2k i32 group counts and cursors
     DevBuf xbfp;         // n x mp bf16 + n f32: the BF16 series and norms in position order
     DevBuf tmask;        // one u64 centroid mask per 128-row tile
+    DevBuf memo_labels;  // n i32: the labels of the previous extraction (memo of unchanged clusters)
+    DevBuf memo_c;       // 3 x k x m f32: that extraction's input and output centroids, this one's input
+    DevBuf memo_flags;   // 3k u8 (dirty, skip, gate for the shift pass) + an i32 valid word
+    DevBuf memo_count;   // 3 u64: extractions with the memo, clusters they covered, clusters skipped
+};
+
+// The extraction's memo (extract.cu): the key of the previous extraction whose
+// labels and centroids the workspace holds; the device word `valid` says whether
+// those are complete.
+struct MemoState {
+    const float* x = nullptr;
+    int64_t n = -1;
+    int m = 0, k = 0, mode = -1, precision = -1, cal_select = -1;
+    bool keyed = false;
+    bool counters = false;  // memo_count allocated and zeroed
 };
 
 // State of the bounded assignment across iterations: the bounds in ws.bounds are
@@ -179,6 +194,8 @@ struct tc_ctx {
     int prep_m = 0;
     // bounded assignment (used for prepared series and inside tc_kshape_run)
     BoundsState bounds;
+    // memo of unchanged clusters in the extraction (same series: prepared, or the run's own)
+    MemoState memo;
 };
 
 namespace tc {
@@ -213,25 +230,22 @@ struct AssignArgs {
     int32_t* cand;
     int32_t* ncand;
     // lower bounds on the exact distance of every (series, centroid) pair, series-major
-    // [n][k] (the bounded assignment across iterations; see assign_fft.cu):
-    //   lb_out  written: the tensor-core pass d16 - lb_d16 for every pair, the FFT passes
-    //           d32 - lb_eps for every pair they evaluate, the bounded pass also the
-    //           carried bounds of the pairs it skips
-    //   lb_in   read by the bounded pass (bounds for the previous centroids), with
-    //           delta[j] >= |c_j/|c_j| - c'_j/|c'_j|| the movement of centroid j; it may
-    //           be lb_out (updated in place)
+    // [n][k] (the bounded assignment across iterations, both forms; see assign_tc.cu):
+    //   lb_out  the tensor-core pass writes d16 - lb_d16 for every pair it evaluates
+    //           and, in a tile-bounded pass, lowers the bounds of the pairs its tile
+    //           skips by delta[j] >= |c_j/|c_j| - c'_j/|c'_j|| (centroid j's movement);
+    //           the FFT pass writes d32 - lb_eps for every pair it evaluates
     float* lb_out;
-    const float* lb_in;
     const float* delta;
     float lb_eps;   // bound on |d32 - d| of the FFT kernel (fft_error)
     float lb_d16;   // bound on |d16 - d| of the tensor-core pass
-    unsigned long long* evals;  // bounded pass: pairs evaluated (accumulated)
-    // tensor-core pass with bounds (BF16 form): per series an upper bound on the exact
-    // distance of its best centroid and that centroid; the tile-bounded pass also
-    // takes the series in position order (xbf, xbf_norm, perm) and a centroid mask
-    // per 128-row tile
+    unsigned long long* evals;  // tile-bounded pass: (tile, centroid) pairs evaluated (accumulated)
+    // tensor-core pass with bounds: per series an upper bound on the exact distance of
+    // its best centroid and that centroid; the tile-bounded pass also takes the series
+    // in position order (xbf, xbf_norm, perm) and a centroid mask per 128-row tile
     float* ubd;
     int32_t* jb;
+    int32_t* gkey;  // full pass before a grouping: best * k + second best, per series
     const void* xbf;
     const float* xbf_norm;
     const int32_t* perm;
@@ -259,17 +273,23 @@ void prepare_series_bf16_reserve(tc_ctx* ctx, int64_t n, int m);
 void prepare_series_bf16_rows(tc_ctx* ctx, const float* x, int64_t n, int m, int64_t r0, int64_t rows,
                               cudaStream_t s);
 void prepare_series_bf16_done(tc_ctx* ctx, const float* x, int64_t n, int m);
-// The tile-bounded BF16 pass's inputs: series grouped by their best centroid jb
-// (perm: position -> series), their BF16 rows and norms in that order, and per
-// 128-row tile the centroids a series of the tile may have as its minimum (k <= 64).
+// The tile-bounded BF16 pass's inputs: series grouped by their best centroid jb as of
+// the last full pass (perm: position -> series), their BF16 rows and norms in that
+// order, and per 128-row tile the centroids a series of the tile may have as its
+// minimum (k <= 64).
 struct TileBounds {
     const int32_t* perm = nullptr;
     const void* xbf = nullptr;
     const float* xbf_norm = nullptr;
     const unsigned long long* tmask = nullptr;
 };
-void launch_tile_bounds(tc_ctx* ctx, int64_t n, int m, int k, const float* lb, const float* ubd, const int32_t* jb,
-                        const float* delta, float D, TileBounds& out, cudaStream_t s);
+// after a full pass: group the series by the best and second best centroids it found
+// (gkey = best * k + second, so groups of one best centroid are adjacent) and copy
+// their BF16 rows in that order; the grouping is kept until the next full pass
+void launch_tile_group(tc_ctx* ctx, int64_t n, int m, int k, const int32_t* gkey, cudaStream_t s);
+// before a bounded pass: the centroid mask of every tile of the kept grouping
+void launch_tile_masks(tc_ctx* ctx, int64_t n, int m, int k, const float* lb, const float* ubd, const int32_t* jb,
+                       const float* delta, float D, TileBounds& out, cudaStream_t s);
 
 // extraction
 struct ExtractArgs {
@@ -280,7 +300,16 @@ struct ExtractArgs {
     int64_t n;
     int m, k, mode, cal_select, precision;
     int32_t* counts;           // k
+    // the series stay fixed across calls (prepared, or the run's own copy): clusters
+    // whose members and centroid equal the previous extraction's reuse its output
+    int memo;
 };
+// Starts the memo for extractions with these arguments: forgets the previous
+// extraction unless it had the same series and shape.  Called outside graph capture
+// (run_extract calls it; the loop calls it once before its captured iterations).
+void memo_prepare(tc_ctx* ctx, const ExtractArgs& a, cudaStream_t s);
+// Forgets the previous extraction (its outputs may be incomplete, or the series changed).
+inline void memo_invalidate(tc_ctx* ctx) { ctx->memo.keyed = false; }
 // no host synchronisation: sum_class and the bad-label flag stay in ws.scal[0..1],
 // the Gram error word at aux+48
 void extract_async(tc_ctx* ctx, const ExtractArgs& a, cudaStream_t s);
@@ -299,9 +328,10 @@ size_t gram_operand_bytes(int64_t n, int k, int m, int precision);
 bool gram_tc_supported(int m, int precision);
 int64_t gram_padded_cols(int64_t n, int k);
 // S_c = YT_c YT_c^T for every cluster (seg == nullptr: the operand is already in place)
+// skip (may be null): clusters whose Gram is not needed (their S is left as it was)
 void launch_gram_tc(tc_ctx* ctx, const float* seg, const int32_t* counts, const int32_t* offsets,
                     const int64_t* poff, int64_t n, int k, int m, int ld, int precision, float* S, int* err,
-                    cudaStream_t s);
+                    cudaStream_t s, const uint8_t* skip = nullptr);
 // power iteration by repeated squaring (power_sq.cu): vec[c] ~ M_c^e v0 where ok[c]
 struct SquaringResult {
     const float* vec = nullptr;  // k x ld, not normalised
@@ -317,7 +347,7 @@ bool gather_transposed_supported(int m);
 void launch_gather_norm_t(const float* x, const int32_t* perm, const int32_t* labels, const int32_t* shift,
                           const uint8_t* gate, const int32_t* offsets, const int32_t* counts, int k,
                           const int64_t* poff, int64_t n, int m, bool bf16, void* YT, float* YTlo, int64_t Pp,
-                          float* first, cudaStream_t s);
+                          float* first, cudaStream_t s, const uint8_t* skip = nullptr);
 
 // workspace of a context: free every buffer (the context must be idle) / bytes held
 void release_workspace(tc_ctx* ctx);

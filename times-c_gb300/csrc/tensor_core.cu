@@ -132,7 +132,7 @@ __global__ void __launch_bounds__(128, 1) k_gram_tc(const __grid_constant__ CUte
                                                     const int32_t* __restrict__ counts,
                                                     const int64_t* __restrict__ poff, int m, int ld, int nt,
                                                     int nsplit, size_t part_stride, float* __restrict__ S,
-                                                    int* __restrict__ err) {
+                                                    int* __restrict__ err, const uint8_t* __restrict__ skip) {
     extern __shared__ uint8_t smem_raw[];
     typedef GtCfg<FMT> G;
     __shared__ __align__(8) uint64_t full[G::STAGES], empty[G::STAGES], done;
@@ -140,7 +140,7 @@ __global__ void __launch_bounds__(128, 1) k_gram_tc(const __grid_constant__ CUte
     uint8_t* base = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
     const int c = blockIdx.y;
     const int cnt = counts[c];
-    if (cnt == 0) return;
+    if (cnt == 0 || (skip && skip[c])) return;
     int t = blockIdx.x, ta = 0;
     while (t >= nt - ta) { t -= nt - ta; ++ta; }
     const int tb = ta + t;
@@ -259,10 +259,11 @@ __global__ void __launch_bounds__(128, 1) k_gram_tc(const __grid_constant__ CUte
 // with no K blocks wrote nothing and are skipped.  Rows a < m, columns < ld (the
 // padding columns are zeros in every partial).
 __global__ void k_gram_sum(const float* __restrict__ P, int nsplit, size_t part_stride,
-                           const int32_t* __restrict__ counts, int KE, int m, int ld, float* __restrict__ S) {
+                           const int32_t* __restrict__ counts, int KE, int m, int ld, float* __restrict__ S,
+                           const uint8_t* __restrict__ skip) {
     const int c = blockIdx.y;
     const int cnt = counts[c];
-    if (cnt == 0) return;
+    if (cnt == 0 || (skip && skip[c])) return;
     const int nk = (cnt + KE - 1) / KE;
     const size_t n4 = (size_t)m * ld / 4, off = (size_t)c * m * ld / 4;
     const float4* P4 = reinterpret_cast<const float4*>(P);
@@ -333,7 +334,7 @@ GramOperand gram_tc_operand(tc_ctx* ctx, int64_t n, int k, int m, int precision)
 // seg == nullptr: the operand was already written by the fused gather.
 void launch_gram_tc(tc_ctx* ctx, const float* seg, const int32_t* counts, const int32_t* offsets,
                     const int64_t* poff, int64_t n, int k, int m, int ld, int precision, float* S, int* err,
-                    cudaStream_t s) {
+                    cudaStream_t s, const uint8_t* skip) {
     const GramOperand op = gram_tc_operand(ctx, n, k, m, precision);
     const int64_t Pp = op.Pp;
     const int fmt = op.fmt;
@@ -381,20 +382,20 @@ void launch_gram_tc(tc_ctx* ctx, const float* seg, const int32_t* counts, const 
     if (fmt == 1) {
         allow_max_dynamic_smem(k_gram_tc<1>);
         k_gram_tc<1><<<grid, 128, GtCfg<1>::SMEM, s>>>(map, map_lo, counts, poff, m, ld, nt, nsplit, part_stride,
-                                                        out, err);
+                                                        out, err, skip);
     } else if (fmt == 2) {
         allow_max_dynamic_smem(k_gram_tc<2>);
         k_gram_tc<2><<<grid, 128, GtCfg<2>::SMEM, s>>>(map, map_lo, counts, poff, m, ld, nt, nsplit, part_stride,
-                                                        out, err);
+                                                        out, err, skip);
     } else {
         allow_max_dynamic_smem(k_gram_tc<3>);
         k_gram_tc<3><<<grid, 128, GtCfg<3>::SMEM, s>>>(map, map_lo, counts, poff, m, ld, nt, nsplit, part_stride,
-                                                        out, err);
+                                                        out, err, skip);
     }
     TC_CHECK_LAUNCH();
     if (nsplit > 1) {
         k_gram_sum<<<dim3(ceil_div((int64_t)m * ld / 4, 256 * 4), k), 256, 0, s>>>(out, nsplit, part_stride, counts,
-                                                                                  KE, m, ld, S);
+                                                                                  KE, m, ld, S, skip);
         TC_CHECK_LAUNCH();
     }
 }

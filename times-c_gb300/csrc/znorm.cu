@@ -227,7 +227,7 @@ __global__ void __launch_bounds__(256) k_gather_norm_t(const float* __restrict__
                                                        const int32_t* __restrict__ counts, int k,
                                                        const int64_t* __restrict__ poff, TO* __restrict__ YT,
                                                        float* __restrict__ YTlo, int64_t Pp,
-                                                       float* __restrict__ first) {
+                                                       float* __restrict__ first, const uint8_t* __restrict__ skip) {
     extern __shared__ float tile[];  // [32][m + 1]
     const int pitch = m + 1;
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
@@ -240,6 +240,7 @@ __global__ void __launch_bounds__(256) k_gather_norm_t(const float* __restrict__
         if (pos >= placed) break;
         const int64_t i = perm[pos];
         const int c = labels[i];
+        if (skip && skip[c]) continue;  // uniform over the warp: one row per warp
         const float* x = src + (size_t)i * m;
         const int sh = (gate && shift && gate[c]) ? shift[i] : 0;
         float v[VPL];
@@ -278,6 +279,7 @@ __global__ void __launch_bounds__(256) k_gather_norm_t(const float* __restrict__
     const int64_t pos = pos0 + r;
     if (pos >= placed) return;
     const int c = labels[perm[pos]];
+    if (skip && skip[c]) return;  // its row was not staged
     const int64_t pp = pos - offsets[c] + poff[c];
     for (int a = wid; a < m; a += 8) {
         const float y = tile[r * pitch + a];
@@ -292,7 +294,7 @@ bool gather_transposed_supported(int m) { return m >= 2 && m <= 1024; }
 void launch_gather_norm_t(const float* x, const int32_t* perm, const int32_t* labels, const int32_t* shift,
                           const uint8_t* gate, const int32_t* offsets, const int32_t* counts, int k,
                           const int64_t* poff, int64_t n, int m, bool bf16, void* YT, float* YTlo, int64_t Pp,
-                          float* first, cudaStream_t s) {
+                          float* first, cudaStream_t s, const uint8_t* skip) {
     if (n == 0) return;
     TC_REQUIRE(gather_transposed_supported(m), TC_ERR_UNSUPPORTED, "fused gather: m must be in [2, 1024]");
     const size_t smem = (size_t)32 * (m + 1) * sizeof(float);
@@ -304,11 +306,12 @@ void launch_gather_norm_t(const float* x, const int32_t* perm, const int32_t* la
             k_gather_norm_t<VPL, __nv_bfloat16><<<grid, 256, smem, s>>>(x, n, m, perm, labels, shift, gate,     \
                                                                         offsets, counts, k, poff,               \
                                                                         (__nv_bfloat16*)YT,                     \
-                                                                        nullptr, Pp, first);                   \
+                                                                        nullptr, Pp, first, skip);             \
         } else {                                                                                                \
             allow_max_dynamic_smem(k_gather_norm_t<VPL, float>);                                                \
             k_gather_norm_t<VPL, float><<<grid, 256, smem, s>>>(x, n, m, perm, labels, shift, gate, offsets,    \
-                                                                counts, k, poff, (float*)YT, YTlo, Pp, first);  \
+                                                                counts, k, poff, (float*)YT, YTlo, Pp, first,   \
+                                                                skip);                                          \
         }                                                                                                       \
     } while (0)
     if (m <= 64) GT(2);

@@ -64,6 +64,8 @@ SIGNATURES = {
     "tc_prepare_series": (_int, [_vp, _vp, _i64, _int, _vp]),
     "tc_assign_stats": (_int, [_vp, ctypes.POINTER(ctypes.c_uint64), ctypes.POINTER(ctypes.c_uint64),
                                ctypes.POINTER(ctypes.c_uint64)]),
+    "tc_extract_stats": (_int, [_vp, ctypes.POINTER(ctypes.c_uint64), ctypes.POINTER(ctypes.c_uint64),
+                                ctypes.POINTER(ctypes.c_uint64)]),
     "tc_sbd_assign_noalloc": (_int, [_vp, _vp, _i64, _int, _int, _int, _vp, _vp, _vp, ctypes.c_char_p, _int]),
     "tc_extract_shapes": (_int, [_vp, _vp, _vp, _vp, _vp, _i64, _int, _int, _int, _int, _int, _vp,
                                  ctypes.POINTER(_int), _vp]),
@@ -168,10 +170,18 @@ class Context:
                                         _ptr(dist_sum), _stream(stream)))
 
     def assign_stats(self):
-        """(screened, bounded, bounded_pairs): FP32 assignments that built distance bounds,
+        """(screened, bounded, bounded_pairs): assignments that built distance bounds,
         that used them, and the (series, centroid) pairs the bounded ones evaluated."""
         a, b, c = ctypes.c_uint64(), ctypes.c_uint64(), ctypes.c_uint64()
         self._check(lib().tc_assign_stats(self.h, ctypes.byref(a), ctypes.byref(b), ctypes.byref(c)))
+        return a.value, b.value, c.value
+
+    def extract_stats(self):
+        """(extractions, clusters, reused): extractions that compared their clusters with
+        the previous call's, the clusters they covered, and those whose output was
+        reused unchanged (synchronises the device)."""
+        a, b, c = ctypes.c_uint64(), ctypes.c_uint64(), ctypes.c_uint64()
+        self._check(lib().tc_extract_stats(self.h, ctypes.byref(a), ctypes.byref(b), ctypes.byref(c)))
         return a.value, b.value, c.value
 
     def prepare_series(self, x, stream=None):
