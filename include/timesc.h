@@ -119,8 +119,9 @@ int tc_prepare_series(tc_ctx* ctx, const float* d_x, int64_t n, int m, tc_stream
  * the pairs whose bound does not rule them out, per 128-series tile of series
  * grouped by their best centroid (in TC_PREC_FP32 that tile-bounded BF16 pass is the
  * screen, and the FP32 pass evaluates its candidates) - with labels and distances
- * equal to evaluating every pair.  A call that evaluated more
- * than 30% of its pairs makes the next one a full call.  screened: calls that built
+ * equal to evaluating every pair.  A full call runs again once the bounded calls
+ * since the last one have cost about one full call more than the cheapest of them
+ * would have.  screened: calls that built
  * bounds; bounded: calls that used them; bounded_pairs: pairs those evaluated (out
  * of n*k each, counted in whole 128-series tiles).  Any output may be NULL.
  * TIMESC_NO_BOUNDS=1 in the environment turns the bounds off.  No counterpart in

@@ -35,7 +35,7 @@ def _run(ctx, data, k, mode, init_chose, seed, bounds, prec=0, cap=30):
     (0, 2000, 100, 5, 0),      # compat pad-with-2 (2m - 1 < 512)
     (0, 4000, 300, 8, 1),      # compat, raw-row start
     (1, 3000, 200, 6, 0),      # canonical, F = 512
-    (1, 3000, 400, 6, 1),      # canonical, F = 1024
+    (1, 3000, 400, 6, 0),      # canonical, F = 1024
     (0, 8000, 512, 32, 0),     # the precision configuration's shape, smaller n
 ])
 def test_loop_with_bounds_equals_dense(built, prec, mode, n, m, k, init_chose):

@@ -51,15 +51,27 @@ static void check_shape(int64_t n, int m, int k, int mode) {
                "FFT length " + std::to_string(F) + " outside [8, 16384] (series too short or too long for this mode)");
 }
 
-// The bounded assignment across iterations (FP32 form, at the lengths the tensor-core
-// screen takes): lower bounds on every (series, centroid) distance, carried from one
-// assignment to the next with each centroid's movement, let the FFT pass skip the
-// pairs that cannot be a series' first minimum.  Bounds are kept only for series that
-// stay fixed across calls - those prepared by tc_prepare_series (or the whole loop's
-// own normalised copy) - and are rebuilt by the screened pass whenever the bounded
-// pass had to evaluate more than BOUNDS_REFRESH_FRACTION of the pairs.
-enum { BOUNDS_OFF = 0, BOUNDS_AUTO = -1, BOUNDS_REFRESH = 1, BOUNDS_USE = 2 };
-constexpr double BOUNDS_REFRESH_FRACTION = 0.3;
+// The bounded assignment across iterations (both forms, at the lengths the tensor-core
+// correlation takes): lower bounds on every (series, centroid) distance, carried from
+// one assignment to the next with each centroid's movement, let the tensor-core pass
+// skip, per 128-series tile, the centroids that cannot be any of the tile's series'
+// first minimum.  Bounds are kept only for series that stay fixed across calls - those
+// prepared by tc_prepare_series (or the whole loop's own normalised copy).
+//   * A full pass (BOUNDS_REFRESH) evaluates every pair, writes fresh bounds and
+//     groups the series by best and second-best centroid.
+//   * A bounded pass (BOUNDS_USE) evaluates the tiles' masks; BOUNDS_USE_REGROUP first
+//     groups the series anew by the keys the previous pass left, which the next pass
+//     does once more than 1/200 of the series changed their best centroid since the
+//     last grouping (a moved series widens its old tile's mask).
+//   * Every evaluated pair gets a fresh bound, so only the skipped ones loosen; a full
+//     pass is run again once the bounded passes since the last one have cost, beyond
+//     the cheapest of them, about one full pass (in units of a full tensor-core pass:
+//     sum of evaluated fractions - passes x their minimum >= BOUNDS_REFRESH_COST).
+enum { BOUNDS_OFF = 0, BOUNDS_AUTO = -1, BOUNDS_REFRESH = 1, BOUNDS_USE = 2, BOUNDS_USE_REGROUP = 3 };
+constexpr double BOUNDS_REFRESH_COST = 1.0;
+constexpr int64_t BOUNDS_REGROUP_SHARE = 200;
+
+static bool bounded_mode(int use) { return use == BOUNDS_USE || use == BOUNDS_USE_REGROUP; }
 
 // Bounds are kept for the FP32 form where the screened pass runs, and for the BF16
 // form where the tensor-core correlation runs with k <= 64 (one mask word per tile).
@@ -91,6 +103,46 @@ static BoundsState& bounds_for(tc_ctx* ctx, const float* x, int64_t n, int m, in
     return b;
 }
 
+// The mode an assignment with bounds runs in (bmode AUTO: from the state).
+static int bounds_mode(const BoundsState& b, int bmode) {
+    int use = bmode;
+    if (bmode == BOUNDS_AUTO) use = b.refresh ? BOUNDS_REFRESH : (b.regroup ? BOUNDS_USE_REGROUP : BOUNDS_USE);
+    if (bounded_mode(use) && !b.valid) use = BOUNDS_REFRESH;
+    return use;
+}
+
+// The bound fields of one tensor-core pass and what runs before it: centroid
+// movements, counters, and for a bounded pass the (new) grouping and the tile masks.
+static void bounds_setup(tc_ctx* ctx, AssignArgs& a, int use, const float* C, cudaStream_t s) {
+    Workspace& ws = ctx->ws;
+    const int64_t n = a.n;
+    const int m = a.m, k = a.k;
+    float* cprev = ws.cprev.as<float>((size_t)k * m + k);
+    float* delta = cprev + (size_t)k * m;
+    launch_centroid_delta(C, k, m, cprev, delta, s);  // cprev <- these centroids
+    char* st = static_cast<char*>(ws.bstate.get((size_t)n * 12));
+    a.ubd = reinterpret_cast<float*>(st);
+    a.jb = reinterpret_cast<int32_t*>(st + (size_t)n * 4);
+    a.gkey = reinterpret_cast<int32_t*>(st + (size_t)n * 8);
+    a.lb_out = ws.bounds.as<float>((size_t)k * n);  // the BF16 pass d16 - D, an FP32 pass d32 - eps
+    a.lb_d16 = (float)bf16_error(m, a.F);
+    a.lb_eps = (float)(fft_error(m, a.F) + 1e-6);
+    unsigned long long* cnt = reinterpret_cast<unsigned long long*>(ws.aux.as<char>(64) + 24);
+    TC_CUDA(cudaMemsetAsync(cnt, 0, 2 * sizeof(unsigned long long), s));  // evaluated tiles, moved series
+    a.moved = cnt + 1;
+    if (bounded_mode(use)) {
+        if (use == BOUNDS_USE_REGROUP) launch_tile_group(ctx, n, m, k, a.gkey, s);
+        TileBounds tb;
+        launch_tile_masks(ctx, n, m, k, a.lb_out, a.ubd, a.jb, delta, a.lb_d16, tb, s);
+        a.perm = tb.perm;
+        a.xbf = tb.xbf;
+        a.xbf_norm = tb.xbf_norm;
+        a.tmask = tb.tmask;
+        a.delta = delta;
+        a.evals = cnt;
+    }
+}
+
 // One assignment against the current centroids.  Returns the bounds mode it ran.
 static int assign(tc_ctx* ctx, const float* x, const float* C, int64_t n, int m, int k, int mode, int precision,
                   int32_t* labels, float* dist, int32_t* shift, const int32_t* old, int32_t* changed,
@@ -120,36 +172,11 @@ static int assign(tc_ctx* ctx, const float* x, const float* C, int64_t n, int m,
         Workspace& ws = ctx->ws;
         const bool usable = bmode != BOUNDS_OFF && bounds_usable(ctx, x, n, m, k, mode, precision);
         BoundsState& b = usable ? bounds_for(ctx, x, n, m, k, mode, precision) : ctx->bounds;
-        int use = BOUNDS_OFF;
-        if (usable) use = bmode == BOUNDS_AUTO ? (b.valid && !b.refresh ? BOUNDS_USE : BOUNDS_REFRESH) : bmode;
-        if (use == BOUNDS_USE && !b.valid) use = BOUNDS_REFRESH;
+        const int use = usable ? bounds_mode(b, bmode) : BOUNDS_OFF;
         a.centroids = C;
         a.cand = ws.screen.as<int32_t>((size_t)n * (SCREEN_CAP + 1));
         a.ncand = a.cand + (size_t)n * SCREEN_CAP;
-        if (use != BOUNDS_OFF) {
-            float* cprev = ws.cprev.as<float>((size_t)k * m + k);
-            float* delta = cprev + (size_t)k * m;
-            launch_centroid_delta(C, k, m, cprev, delta, s);  // cprev <- these centroids
-            char* st = static_cast<char*>(ws.bstate.get((size_t)n * 12));
-            a.ubd = reinterpret_cast<float*>(st);
-            a.jb = reinterpret_cast<int32_t*>(st + (size_t)n * 4);
-            if (use == BOUNDS_REFRESH) a.gkey = reinterpret_cast<int32_t*>(st + (size_t)n * 8);
-            a.lb_out = ws.bounds.as<float>((size_t)k * n);  // the BF16 pass d16 - D, the FP32 pass d32 - eps
-            a.lb_d16 = (float)bf16_error(m, F);
-            a.lb_eps = (float)(fft_error(m, F) + 1e-6);
-            if (use == BOUNDS_USE) {
-                unsigned long long* evals = reinterpret_cast<unsigned long long*>(ws.aux.as<char>(64) + 24);
-                TC_CUDA(cudaMemsetAsync(evals, 0, sizeof(unsigned long long), s));
-                TileBounds tb;
-                launch_tile_masks(ctx, n, m, k, a.lb_out, a.ubd, a.jb, delta, a.lb_d16, tb, s);
-                a.perm = tb.perm;
-                a.xbf = tb.xbf;
-                a.xbf_norm = tb.xbf_norm;
-                a.tmask = tb.tmask;
-                a.delta = delta;
-                a.evals = evals;
-            }
-        }
+        if (use != BOUNDS_OFF) bounds_setup(ctx, a, use, C, s);
         // -1 (all centroids) for every series the tensor-core pass does not reach,
         // e.g. after one of its bounded waits ran out
         TC_CUDA(cudaMemsetAsync(a.ncand, 0xFF, (size_t)n * sizeof(int32_t), s));
@@ -182,56 +209,42 @@ static int assign(tc_ctx* ctx, const float* x, const float* C, int64_t n, int m,
     // per series an upper bound on its best, and groups the series by that best; the
     // tile-bounded passes then evaluate, per 128-row tile of that grouping, only the
     // centroids whose bounds do not rule them out for every series of the tile
-    Workspace& ws = ctx->ws;
     BoundsState& b = bounds_for(ctx, x, n, m, k, mode, precision);
-    int use = bmode == BOUNDS_AUTO ? (b.valid && !b.refresh ? BOUNDS_USE : BOUNDS_REFRESH) : bmode;
-    if (use == BOUNDS_USE && !b.valid) use = BOUNDS_REFRESH;
-    float* lb = ws.bounds.as<float>((size_t)k * n);
-    float* cprev = ws.cprev.as<float>((size_t)k * m + k);
-    float* delta = cprev + (size_t)k * m;
-    char* st = static_cast<char*>(ws.bstate.get((size_t)n * 12));
-    a.ubd = reinterpret_cast<float*>(st);
-    a.jb = reinterpret_cast<int32_t*>(st + (size_t)n * 4);
-    if (use == BOUNDS_REFRESH) a.gkey = reinterpret_cast<int32_t*>(st + (size_t)n * 8);
-    a.lb_out = lb;
-    a.lb_d16 = (float)bf16_error(m, F);
-    launch_centroid_delta(C, k, m, cprev, delta, s);  // cprev <- these centroids
-    if (use == BOUNDS_USE) {
-        unsigned long long* evals = reinterpret_cast<unsigned long long*>(ws.aux.as<char>(64) + 24);
-        TC_CUDA(cudaMemsetAsync(evals, 0, sizeof(unsigned long long), s));
-        TileBounds tb;
-        launch_tile_masks(ctx, n, m, k, lb, a.ubd, a.jb, delta, a.lb_d16, tb, s);
-        a.perm = tb.perm;
-        a.xbf = tb.xbf;
-        a.xbf_norm = tb.xbf_norm;
-        a.tmask = tb.tmask;
-        a.delta = delta;
-        a.evals = evals;
-    }
+    const int use = bounds_mode(b, bmode);
+    bounds_setup(ctx, a, use, C, s);
     launch_assign_tc(ctx, a, precision, s);
     if (use == BOUNDS_REFRESH) {
-        // the bounded passes until the next full one keep this grouping (by best and
-        // second best: series with both in common have similar masks); a series whose
-        // best centroid changes stays in its tile, which only widens that tile's mask
-        launch_tile_group(ctx, n, m, k, a.gkey, s);
+        launch_tile_group(ctx, n, m, k, a.gkey, s);  // by best and second best: similar masks
         b.valid = true;
         b.refresh = false;
     }
     return use;
 }
 
-// After an assignment that kept bounds: count it, and after a bounded pass rebuild
-// the bounds next time if it evaluated too many pairs.
-static void bounds_feedback(tc_ctx* ctx, int used, unsigned long long evals, int64_t n, int k) {
+// After an assignment that kept bounds: count it, and decide whether the next one
+// regroups the series or runs a full pass (see BOUNDS_REFRESH_COST).
+static void bounds_feedback(tc_ctx* ctx, int used, unsigned long long evals, unsigned long long moved, int64_t n,
+                            int k) {
     BoundsState& b = ctx->bounds;
     if (used == BOUNDS_REFRESH) {
         ++b.screened;
-    } else if (used == BOUNDS_USE) {
+        b.moved = 0;  // grouped by this pass's keys
+        b.regroup = false;
+        b.sum_f = 0;
+        b.min_f = 2;
+        b.passes = 0;
+    } else if (bounded_mode(used)) {
         // the tensor-core pass counts (tile, centroid) pairs of its 128-row tiles
         evals *= 128;
         ++b.bounded;
         b.bounded_pairs += evals;
-        b.refresh = (double)evals > BOUNDS_REFRESH_FRACTION * (double)n * k;
+        b.moved = (used == BOUNDS_USE_REGROUP ? 0 : b.moved) + moved;
+        b.regroup = (int64_t)b.moved * BOUNDS_REGROUP_SHARE > n;
+        const double f = (double)evals / ((double)n * k);
+        b.sum_f += f;
+        b.min_f = std::min(b.min_f, f);
+        ++b.passes;
+        b.refresh = b.sum_f - b.passes * b.min_f >= BOUNDS_REFRESH_COST;
     }
 }
 
@@ -347,18 +360,20 @@ static LoopState run_loop(tc_ctx* ctx, const tc_job* job, const float* x, int k,
     double old_inertia = 1e10;
     int countIter = 0;
     // what the stages leave in aux: changed (+0), dist sum (+8), sum_class and the
-    // bad-label flag (+16), error words of the Gram and the correlation (+48)
+    // bad-label flag (+16), the bounded pass's counters (+24, +32), error words of the
+    // Gram and the correlation (+48)
     struct {
         int32_t changed;
         int32_t pad;
         double dsum;
         int32_t sum_class, bad_label;
-        unsigned long long evals;  // pairs the bounded pass evaluated (+24)
-        int32_t pad2[4];
+        unsigned long long evals;  // (tile, centroid) pairs the bounded pass evaluated (+24)
+        unsigned long long moved;  // series whose best centroid changed (+32)
+        int32_t pad2[2];
         int32_t err[2];
     } h;
     static_assert(sizeof(h) == 56, "aux layout");
-    StageGraph g_extract, g_assign, g_assign_bounded;
+    StageGraph g_extract, g_assign, g_assign_bounded, g_assign_regroup;
     const bool bnd = bounds_usable(ctx, x, n, m, k, job->mode, job->precision);
     const bool graphs = ctx->graphs && !std::getenv("TIMESC_NO_GRAPHS");
     auto readback = [&]() {
@@ -396,18 +411,19 @@ static LoopState run_loop(tc_ctx* ctx, const tc_job* job, const float* x, int k,
         TC_CUDA(cudaMemcpyAsync(aux + 16, ws.scal.p, 2 * sizeof(int32_t), cudaMemcpyDeviceToDevice, s));
     };
     auto do_assign = [&]() -> bool {
-        // the bounded pass while the bounds are valid and last pass evaluated few pairs;
-        // the screened pass (rebuilding the bounds) otherwise - one graph for each
-        const bool use_b = bnd && ctx->bounds.valid && !ctx->bounds.refresh;
-        if (use_b) g_assign_bounded.run(graphs, s, [&]() { issue_assign(BOUNDS_USE); });
+        // a full pass (or no bounds), a bounded pass, or a bounded pass on a new
+        // grouping, as the bounds state asks - one graph for each
+        const int use = bnd ? bounds_mode(ctx->bounds, BOUNDS_AUTO) : BOUNDS_OFF;
+        if (use == BOUNDS_USE) g_assign_bounded.run(graphs, s, [&]() { issue_assign(BOUNDS_USE); });
+        else if (use == BOUNDS_USE_REGROUP) g_assign_regroup.run(graphs, s, [&]() { issue_assign(BOUNDS_USE_REGROUP); });
         else g_assign.run(graphs, s, [&]() { issue_assign(BOUNDS_REFRESH); });
         readback();
         if (bnd) {
-            if (!use_b) {
+            if (use == BOUNDS_REFRESH) {
                 ctx->bounds.valid = true;
                 ctx->bounds.refresh = false;
             }
-            bounds_feedback(ctx, use_b ? BOUNDS_USE : BOUNDS_REFRESH, h.evals, n, k);
+            bounds_feedback(ctx, use, h.evals, h.moved, n, k);
         }
         check_guards(ctx, "assignment");
         st.inertia = h.dsum / (double)n;
@@ -630,8 +646,8 @@ int tc_sbd_assign(tc_ctx* ctx, const float* d_x, const float* d_centroids, int64
     const bool tc_used = precision != TC_PREC_FP32 || (!d_shift && screen_supported(m, fft_size(m, mode), k));
     if (tc_used) {  // the tensor-core pass reports through an error word; the bounded pass counts its pairs
         struct {
-            unsigned long long evals;
-            int32_t pad[4];
+            unsigned long long evals, moved;
+            int32_t pad[2];
             int32_t err[2];
         } h;
         static_assert(sizeof(h) == 32, "aux layout");
@@ -639,7 +655,7 @@ int tc_sbd_assign(tc_ctx* ctx, const float* d_x, const float* d_centroids, int64
         TC_CUDA(cudaStreamSynchronize(s));
         if (h.err[0] || h.err[1]) ctx->bounds.valid = false;  // a pass that stopped early left no bounds
         check_async_errors(h.err);
-        bounds_feedback(ctx, used, h.evals, n, k);
+        bounds_feedback(ctx, used, h.evals, h.moved, n, k);
     }
     TC_API_END(ctx)
 }

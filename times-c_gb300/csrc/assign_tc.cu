@@ -169,8 +169,9 @@ struct AtParams {
     // centroid, and that centroid (the bounded BF16 pass reads and rewrites them)
     float* ubd;
     int32_t* jb;
-    // full pass before a grouping: per series best * k + second best (the group key)
+    // per series best * k + second best (the group key of the next grouping)
     int32_t* gkey;
+    unsigned long long* moved;  // series whose best centroid differs from jb's old value
     // tile-bounded pass: the tiles hold cluster-grouped positions (perm maps a position
     // to its series, for the outputs and bounds); only the centroids of tmask[tile]
     // are evaluated, and the other bounds of the tile's series are carried down by
@@ -345,7 +346,7 @@ __global__ void __launch_bounds__(AT_THREADS, 1) k_assign_tc(const __grid_consta
         const uint32_t tq = tmem + ((uint32_t)(quarter * 32) << 16);
         const int nchunk = g.NG / 32;  // 4 or 8
         double dsum = 0.0;
-        int nchg = 0;
+        int nchg = 0, nmov = 0;
         int64_t q = 0;
         for (int64_t tile = blockIdx.x; tile < ntiles && ok; tile += gridDim.x) {
             const int64_t pos = tile * AT_TILE + row;  // the tile row (a series position)
@@ -436,6 +437,7 @@ __global__ void __launch_bounds__(AT_THREADS, 1) k_assign_tc(const __grid_consta
                     }
                 }
                 if (p.ubd) {
+                    if (p.moved && p.jb[i] != bestj) ++nmov;
                     p.ubd[i] = __fadd_ru(bestd, p.lb_d16);
                     p.jb[i] = bestj;
                 }
@@ -458,10 +460,12 @@ __global__ void __launch_bounds__(AT_THREADS, 1) k_assign_tc(const __grid_consta
         for (int o = 16; o > 0; o >>= 1) {
             dsum += __shfl_xor_sync(0xffffffffu, dsum, o);
             nchg += __shfl_xor_sync(0xffffffffu, nchg, o);
+            nmov += __shfl_xor_sync(0xffffffffu, nmov, o);
         }
         if (lane == 0) {
             if (p.dist_sum) atomicAdd(p.dist_sum, dsum);
             if (p.changed && nchg) atomicAdd(p.changed, nchg);
+            if (p.moved && nmov) atomicAdd(p.moved, (unsigned long long)nmov);
         }
     }
     sm100::tc_fence_before();
@@ -763,6 +767,7 @@ void launch_assign_tc(tc_ctx* ctx, const AssignArgs& a, int precision, cudaStrea
     p.ubd = a.ubd;
     p.jb = a.jb;
     p.gkey = a.gkey;
+    p.moved = a.moved;
     p.tmask = a.tmask;
     p.perm = a.perm;
     p.delta = a.delta;

@@ -79,8 +79,12 @@ __device__ __forceinline__ double rsqrt_d(double x) {
 // BPL > 0: rows of at most 32*BPL float4 (loads unrolled); 0: any length.
 // RES: the CTA's rows of S_c are copied into shared memory once and every step reads
 // them there (when they fit: m <= ~600 with 8 CTAs per cluster), else from L2.
-template <int CL, int BPL, bool RES>
+// HOLD (BPL <= 4, at most one group of rows per warp: m <= 512 with 8 CTAs): each
+// warp loads its rows into registers once and keeps them for every step, so a step
+// reads only the vector from shared memory (the rows are 128 KB per CTA a step).
+template <int CL, int BPL, bool RES, bool HOLD>
 __global__ void __launch_bounds__(PC_THREADS, 1) k_power_cluster(PowerClusterParams p) {
+    static_assert(!HOLD || (BPL > 0 && BPL <= 4 && !RES), "HOLD keeps at most 4 x 4 float4 rows per lane");
     namespace cg = cooperative_groups;
     cg::cluster_group cluster = cg::this_cluster();
     extern __shared__ __align__(16) unsigned char dsm[];
@@ -170,16 +174,25 @@ __global__ void __launch_bounds__(PC_THREADS, 1) k_power_cluster(PowerClusterPar
         for (int a = threadIdx.x; a < 2 * ld; a += PC_THREADS) ybuf[a] = 0.f;  // padding stays zero
         __syncthreads();
     }
-    float* yrem[CL];
-    float2* prem[CL];
+    // lane q < CL stores into CTA q: one remote address per lane
+    float* yre = cluster.map_shared_rank(ybuf, lane < CL ? lane : 0);
+    float2* pre = cluster.map_shared_rank(part, lane < CL ? lane : 0);
+    constexpr int U = BPL >= 8 ? 2 : PC_UNROLL;  // rows in flight per warp
+    constexpr int XU = HOLD ? U : 1, XB = HOLD ? BPL : 1;
+    float4 xh[XU][XB];  // HOLD: this warp's rows wid*U.., loaded once
+    if constexpr (HOLD) {
 #pragma unroll
-    for (int q = 0; q < CL; ++q) {
-        yrem[q] = cluster.map_shared_rank(ybuf, q);
-        prem[q] = cluster.map_shared_rank(part, q);
+        for (int u = 0; u < U; ++u)
+#pragma unroll
+            for (int j = 0; j < BPL; ++j) {
+                const int i = wid * U + u, b = lane + 32 * j;
+                xh[u][j] = (i < nrow && b < nv4)
+                               ? __ldg(reinterpret_cast<const float4*>(Sc + (size_t)(a0 + i) * ld) + b)
+                               : make_float4(0.f, 0.f, 0.f, 0.f);
+            }
     }
     cluster.sync();  // every CTA initialised before remote stores start
     int T = tmax;
-    constexpr int U = BPL >= 8 ? 2 : PC_UNROLL;  // rows in flight per warp
     float fsc = 1.f;  // v_t = ybuf[(t-1)&1] * fsc for t >= 1 (the FP32 product the update stored before)
     for (int t = 0;; ++t) {
         const int par = t & 1;
@@ -211,7 +224,21 @@ __global__ void __launch_bounds__(PC_THREADS, 1) k_power_cluster(PowerClusterPar
                 cp[u] = (tt - s[u]) - yk;
                 s[u] = tt;
             };
-            if constexpr (BPL > 0) {
+            if constexpr (HOLD) {
+#pragma unroll
+                for (int j = 0; j < BPL; ++j) {
+                    const int b = lane + 32 * j;
+                    if (b < nv4) {
+                        float4 w = vt4[b];
+                        w.x *= fsc;
+                        w.y *= fsc;
+                        w.z *= fsc;
+                        w.w *= fsc;
+#pragma unroll
+                        for (int u = 0; u < U; ++u) kahan4(u, xh[u][j], w);
+                    }
+                }
+            } else if constexpr (BPL > 0) {
                 // every load of the U rows in flight at once: one L2 round trip per step
                 float4 x[U][BPL];
 #pragma unroll
@@ -261,7 +288,7 @@ __global__ void __launch_bounds__(PC_THREADS, 1) k_power_cluster(PowerClusterPar
                     const int a = a0 + i;
                     const float ra = r_own[i];
                     const float yf = (s[u] - cp[u]) + fmaf(cr, ra, cc);
-                    if (lane < CL) yrem[lane][par * ld + a] = yf;  // into every CTA of the cluster
+                    if (lane < CL) yre[par * ld + a] = yf;  // into every CTA of the cluster
                     if (lane == 0) {
                         add_prod(0, yf, yf);
                         two_sum_acc(accs[1], accc[1], yf, 0.f);
@@ -283,7 +310,7 @@ __global__ void __launch_bounds__(PC_THREADS, 1) k_power_cluster(PowerClusterPar
         for (int q = 0; q < 4; ++q)
             mine[q] = make_float2(__shfl_sync(0xffffffffu, accs[q], 0), __shfl_sync(0xffffffffu, accc[q], 0));
         if (lane < CL) {
-            float2* dst = prem[lane] + ((size_t)(par * CL + rank) * NWARP + wid) * 4;
+            float2* dst = pre + ((size_t)(par * CL + rank) * NWARP + wid) * 4;
 #pragma unroll
             for (int q = 0; q < 4; ++q) dst[q] = mine[q];
         }
@@ -403,9 +430,9 @@ __global__ void __launch_bounds__(PC_THREADS, 1) k_power_cluster(PowerClusterPar
 }
 
 // ---------------------------------------------------------------- host
-template <int CL, int BPL, bool RES>
+template <int CL, int BPL, bool RES, bool HOLD = false>
 static void launch_cluster(const PowerClusterParams& pp, int k, size_t smem, cudaStream_t s) {
-    auto kern = k_power_cluster<CL, BPL, RES>;
+    auto kern = k_power_cluster<CL, BPL, RES, HOLD>;
     allow_max_dynamic_smem(kern);
     if (CL > 8) TC_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
     cudaLaunchConfig_t cfg = {};
@@ -448,10 +475,17 @@ void power_eigvecs(tc_ctx* ctx, const float* S, int ld, const double* r, const d
         launch_cluster<16, 0, false>(pp, k, smem, s);
     } else {
         const int nv4 = ld / 4;
-        // rows resident in shared memory when they fit (4 KB left for the static arrays)
+        // rows in registers when every warp holds at most one group of 4 rows of at most
+        // 128 float4 (m <= 512); else resident in shared memory when they fit (4 KB left
+        // for the static arrays)
+        const bool hold = (m + 7) / 8 <= (PC_THREADS / 32) * PC_UNROLL && nv4 <= 128;
         const bool res = cluster_smem<8>(m, ld, true) + 4096 <= ctx->smem_optin && !std::getenv("TIMESC_POWER_L2");
-        const size_t smem = cluster_smem<8>(m, ld, res);
-        if (res) {
+        const size_t smem = cluster_smem<8>(m, ld, res && !hold);
+        if (hold) {
+            if (nv4 <= 32) launch_cluster<8, 1, false, true>(pp, k, smem, s);
+            else if (nv4 <= 64) launch_cluster<8, 2, false, true>(pp, k, smem, s);
+            else launch_cluster<8, 4, false, true>(pp, k, smem, s);
+        } else if (res) {
             if (nv4 <= 32) launch_cluster<8, 1, true>(pp, k, smem, s);
             else if (nv4 <= 64) launch_cluster<8, 2, true>(pp, k, smem, s);
             else if (nv4 <= 128) launch_cluster<8, 4, true>(pp, k, smem, s);

@@ -170,7 +170,12 @@ struct BoundsState {
     int64_t n = 0;
     int m = 0, k = 0, mode = -1, precision = -1;
     bool valid = false;
-    bool refresh = true;  // next assignment: the screened pass (new bounds)
+    bool refresh = true;   // next assignment: a full pass (new bounds)
+    bool regroup = false;  // next bounded pass: group the series anew first
+    uint64_t moved = 0;    // series whose best centroid changed since the last grouping
+    // bounded passes since the last full pass: their evaluated fractions' sum, count, minimum
+    double sum_f = 0, min_f = 2;
+    int passes = 0;
     // totals for tc_assign_stats
     uint64_t screened = 0, bounded = 0, bounded_pairs = 0;
 };
@@ -245,7 +250,8 @@ struct AssignArgs {
     // in position order (xbf, xbf_norm, perm) and a centroid mask per 128-row tile
     float* ubd;
     int32_t* jb;
-    int32_t* gkey;  // full pass before a grouping: best * k + second best, per series
+    int32_t* gkey;  // per series best * k + second best: the key of the next grouping
+    unsigned long long* moved;  // series whose best centroid changed (accumulated)
     const void* xbf;
     const float* xbf_norm;
     const int32_t* perm;
