@@ -113,13 +113,24 @@ static int bounds_mode(const BoundsState& b, int bmode) {
 
 // The bound fields of one tensor-core pass and what runs before it: centroid
 // movements, counters, and for a bounded pass the (new) grouping and the tile masks.
-static void bounds_setup(tc_ctx* ctx, AssignArgs& a, int use, const float* C, cudaStream_t s) {
+static void bounds_setup(tc_ctx* ctx, AssignArgs& a, int use, const float* C, cudaStream_t s, bool fp32) {
     Workspace& ws = ctx->ws;
     const int64_t n = a.n;
     const int m = a.m, k = a.k;
     float* cprev = ws.cprev.as<float>((size_t)k * m + k);
     float* delta = cprev + (size_t)k * m;
-    launch_centroid_delta(C, k, m, cprev, delta, s);  // cprev <- these centroids
+    float* craw = nullptr;
+    uint8_t* same = nullptr;
+    if (fp32) {  // the FFT pass's labels and distances, and the raw centroids they belong to
+        char* f = static_cast<char*>(ws.fprev.get((size_t)n * 8 + (size_t)k * m * 4 + k));
+        a.prev_dist = reinterpret_cast<float*>(f);
+        a.prev_label = reinterpret_cast<int32_t*>(f + (size_t)n * 4);
+        craw = reinterpret_cast<float*>(f + (size_t)n * 8);
+        same = reinterpret_cast<uint8_t*>(f + (size_t)n * 8 + (size_t)k * m * 4);
+        a.same = same;
+        a.reuse = bounded_mode(use);  // after a full pass every series has its label and distance
+    }
+    launch_centroid_delta(C, k, m, cprev, delta, s, craw, same);  // cprev (and craw) <- these centroids
     char* st = static_cast<char*>(ws.bstate.get((size_t)n * 12));
     a.ubd = reinterpret_cast<float*>(st);
     a.jb = reinterpret_cast<int32_t*>(st + (size_t)n * 4);
@@ -128,12 +139,12 @@ static void bounds_setup(tc_ctx* ctx, AssignArgs& a, int use, const float* C, cu
     a.lb_d16 = (float)bf16_error(m, a.F);
     a.lb_eps = (float)(fft_error(m, a.F) + 1e-6);
     unsigned long long* cnt = reinterpret_cast<unsigned long long*>(ws.aux.as<char>(64) + 24);
-    TC_CUDA(cudaMemsetAsync(cnt, 0, 2 * sizeof(unsigned long long), s));  // evaluated tiles, moved series
+    TC_CUDA(cudaMemsetAsync(cnt, 0, 3 * sizeof(unsigned long long), s));  // evaluated tiles, moved series, series pairs
     a.moved = cnt + 1;
     if (bounded_mode(use)) {
         if (use == BOUNDS_USE_REGROUP) launch_tile_group(ctx, n, m, k, a.gkey, s);
         TileBounds tb;
-        launch_tile_masks(ctx, n, m, k, a.lb_out, a.ubd, a.jb, delta, a.lb_d16, tb, s);
+        launch_tile_masks(ctx, n, m, k, a.lb_out, a.ubd, a.jb, delta, a.lb_d16, tb, s, cnt + 2);
         a.perm = tb.perm;
         a.xbf = tb.xbf;
         a.xbf_norm = tb.xbf_norm;
@@ -176,7 +187,7 @@ static int assign(tc_ctx* ctx, const float* x, const float* C, int64_t n, int m,
         a.centroids = C;
         a.cand = ws.screen.as<int32_t>((size_t)n * (SCREEN_CAP + 1));
         a.ncand = a.cand + (size_t)n * SCREEN_CAP;
-        if (use != BOUNDS_OFF) bounds_setup(ctx, a, use, C, s);
+        if (use != BOUNDS_OFF) bounds_setup(ctx, a, use, C, s, true);
         // -1 (all centroids) for every series the tensor-core pass does not reach,
         // e.g. after one of its bounded waits ran out
         TC_CUDA(cudaMemsetAsync(a.ncand, 0xFF, (size_t)n * sizeof(int32_t), s));
@@ -211,7 +222,7 @@ static int assign(tc_ctx* ctx, const float* x, const float* C, int64_t n, int m,
     // centroids whose bounds do not rule them out for every series of the tile
     BoundsState& b = bounds_for(ctx, x, n, m, k, mode, precision);
     const int use = bounds_mode(b, bmode);
-    bounds_setup(ctx, a, use, C, s);
+    bounds_setup(ctx, a, use, C, s, false);
     launch_assign_tc(ctx, a, precision, s);
     if (use == BOUNDS_REFRESH) {
         launch_tile_group(ctx, n, m, k, a.gkey, s);  // by best and second best: similar masks
@@ -223,8 +234,8 @@ static int assign(tc_ctx* ctx, const float* x, const float* C, int64_t n, int m,
 
 // After an assignment that kept bounds: count it, and decide whether the next one
 // regroups the series or runs a full pass (see BOUNDS_REFRESH_COST).
-static void bounds_feedback(tc_ctx* ctx, int used, unsigned long long evals, unsigned long long moved, int64_t n,
-                            int k) {
+static void bounds_feedback(tc_ctx* ctx, int used, unsigned long long evals, unsigned long long moved,
+                            unsigned long long spairs, int64_t n, int k) {
     BoundsState& b = ctx->bounds;
     if (used == BOUNDS_REFRESH) {
         ++b.screened;
@@ -238,6 +249,11 @@ static void bounds_feedback(tc_ctx* ctx, int used, unsigned long long evals, uns
         evals *= 128;
         ++b.bounded;
         b.bounded_pairs += evals;
+        b.series_pairs += spairs;
+        if (std::getenv("TIMESC_TRACE"))
+            std::fprintf(stderr, "timesc: bounded pass%s: tiles evaluate %.3f of the pairs, the series need %.3f\n",
+                         used == BOUNDS_USE_REGROUP ? " (regrouped)" : "", (double)evals / ((double)n * k),
+                         (double)spairs / ((double)n * k));
         b.moved = (used == BOUNDS_USE_REGROUP ? 0 : b.moved) + moved;
         b.regroup = (int64_t)b.moved * BOUNDS_REGROUP_SHARE > n;
         const double f = (double)evals / ((double)n * k);
@@ -367,9 +383,9 @@ static LoopState run_loop(tc_ctx* ctx, const tc_job* job, const float* x, int k,
         int32_t pad;
         double dsum;
         int32_t sum_class, bad_label;
-        unsigned long long evals;  // (tile, centroid) pairs the bounded pass evaluated (+24)
-        unsigned long long moved;  // series whose best centroid changed (+32)
-        int32_t pad2[2];
+        unsigned long long evals;   // (tile, centroid) pairs the bounded pass evaluated (+24)
+        unsigned long long moved;   // series whose best centroid changed (+32)
+        unsigned long long spairs;  // pairs the series' own masks hold (+40)
         int32_t err[2];
     } h;
     static_assert(sizeof(h) == 56, "aux layout");
@@ -423,7 +439,7 @@ static LoopState run_loop(tc_ctx* ctx, const tc_job* job, const float* x, int k,
                 ctx->bounds.valid = true;
                 ctx->bounds.refresh = false;
             }
-            bounds_feedback(ctx, use, h.evals, h.moved, n, k);
+            bounds_feedback(ctx, use, h.evals, h.moved, h.spairs, n, k);
         }
         check_guards(ctx, "assignment");
         st.inertia = h.dsum / (double)n;
@@ -646,8 +662,7 @@ int tc_sbd_assign(tc_ctx* ctx, const float* d_x, const float* d_centroids, int64
     const bool tc_used = precision != TC_PREC_FP32 || (!d_shift && screen_supported(m, fft_size(m, mode), k));
     if (tc_used) {  // the tensor-core pass reports through an error word; the bounded pass counts its pairs
         struct {
-            unsigned long long evals, moved;
-            int32_t pad[2];
+            unsigned long long evals, moved, spairs;
             int32_t err[2];
         } h;
         static_assert(sizeof(h) == 32, "aux layout");
@@ -655,7 +670,7 @@ int tc_sbd_assign(tc_ctx* ctx, const float* d_x, const float* d_centroids, int64
         TC_CUDA(cudaStreamSynchronize(s));
         if (h.err[0] || h.err[1]) ctx->bounds.valid = false;  // a pass that stopped early left no bounds
         check_async_errors(h.err);
-        bounds_feedback(ctx, used, h.evals, h.moved, n, k);
+        bounds_feedback(ctx, used, h.evals, h.moved, h.spairs, n, k);
     }
     TC_API_END(ctx)
 }

@@ -230,6 +230,13 @@ struct AssignParams {
     // lower bounds [n][k] on the exact distances: d32 - lb_eps for every pair evaluated
     float* lb_out;
     float lb_eps;
+    // per series the label and distance this pass leaves (written when set); with
+    // reuse, a series whose only candidate is that label, of a centroid unchanged
+    // (same[j]) since, keeps that distance without being transformed
+    float* prev_dist;
+    int32_t* prev_label;
+    const uint8_t* same;
+    int reuse;
 };
 
 // Max NCC over the valid lags with the lag of the first maximum in sbd3D's order
@@ -285,6 +292,21 @@ __global__ void __launch_bounds__(Cfg<N>::BLOCK, 1) k_assign_fft(AssignParams p)
         if (p.fixed && p.gate && !p.gate[p.fixed[i]]) {  // uniform over the team
             if (tid == 0 && p.shift) p.shift[i] = 0;
             continue;
+        }
+        if (p.reuse) {  // uniform over the team: every thread reads the same values
+            const int32_t* cl = p.cand + (size_t)i * SCREEN_CAP;
+            const int j = cl[0];
+            if (screen_list_len(cl, p.ncand[i], p.k) == 1 && j == p.prev_label[i] && p.same[j]) {
+                if (tid == 0) {  // the distance the same kernel computed for this series and centroid
+                    const float d = p.prev_dist[i];
+                    if (p.labels) p.labels[i] = j;
+                    if (p.dist) p.dist[i] = d;
+                    if (p.lb_out) p.lb_out[(size_t)i * p.k + j] = __fsub_rd(d, p.lb_eps);
+                    dsum += (double)d;
+                    if (p.old_labels && p.old_labels[i] != j) ++nchg;
+                }
+                continue;
+            }
         }
         float2 xh[2][Co::R0];
         float xhN = 0.f;
@@ -357,6 +379,10 @@ __global__ void __launch_bounds__(Cfg<N>::BLOCK, 1) k_assign_fft(AssignParams p)
         if (tid == 0) {
             if (p.labels) p.labels[i] = bestj;
             if (p.dist) p.dist[i] = bestd;
+            if (p.prev_dist) {
+                p.prev_dist[i] = bestd;
+                p.prev_label[i] = bestj;
+            }
             if (p.shift) p.shift[i] = bests;
             dsum += (double)bestd;
             if (p.old_labels && p.old_labels[i] != bestj) ++nchg;
@@ -497,6 +523,11 @@ static void assign_n(tc_ctx* ctx, const AssignArgs& a, cudaStream_t s) {
     p.ncand = a.ncand;
     p.lb_out = a.lb_out;
     p.lb_eps = a.lb_eps;
+    p.prev_dist = a.prev_dist;
+    p.prev_label = a.prev_label;
+    p.same = a.same;
+    p.reuse = a.reuse;
+    TC_REQUIRE(!a.reuse || (a.cand && a.prev_dist && a.same), TC_ERR_ARG, "assignment reuse: arguments");
     const bool want_shift = a.shift != nullptr || a.fixed != nullptr;
     if (want_shift) launch_plan<N, true>(ctx, p, tuned_plan<N, true>(ctx, p, s), s);
     else launch_plan<N, false>(ctx, p, tuned_plan<N, false>(ctx, p, s), s);
@@ -509,18 +540,28 @@ static void assign_n(tc_ctx* ctx, const AssignArgs& a, cudaStream_t s) {
 // unit centroid (zeros for a zero centroid).  The NCC of a series with c_j moves by
 // at most delta[j] at every lag (the lags are norm-preserving or norm-reducing
 // shifts of the unit centroid, Cauchy-Schwarz), and so does its distance.
+// With craw: same[j] = 1 where centroid j equals craw_j bitwise, then craw_j <- c_j.
 __global__ void __launch_bounds__(256) k_centroid_delta(const float* __restrict__ C, int m, float* __restrict__ cprev,
-                                                        float* __restrict__ delta) {
+                                                        float* __restrict__ delta, float* __restrict__ craw,
+                                                        uint8_t* __restrict__ same) {
     __shared__ double red[8][2];
     __shared__ double sh[2];
     const int j = blockIdx.x, lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
     const float* c = C + (size_t)j * m;
     float* cp = cprev + (size_t)j * m;
     double a = 0, b = 0;
+    bool eq = true;
     for (int t = threadIdx.x; t < m; t += 256) {
         a += (double)c[t] * c[t];
         b += (double)cp[t] * cp[t];
+        if (craw) {
+            const float v = c[t];
+            eq = eq && __float_as_uint(v) == __float_as_uint(craw[(size_t)j * m + t]);
+            craw[(size_t)j * m + t] = v;  // this thread's own element: read before written
+        }
     }
+    eq = __syncthreads_and(eq) != 0;
+    if (craw && threadIdx.x == 0) same[j] = eq;
     for (int o = 16; o > 0; o >>= 1) {
         a += __shfl_xor_sync(0xffffffffu, a, o);
         b += __shfl_xor_sync(0xffffffffu, b, o);
@@ -560,8 +601,9 @@ __global__ void __launch_bounds__(256) k_centroid_delta(const float* __restrict_
     for (int t = threadIdx.x; t < m; t += 256) cp[t] = nc > 0 ? (float)((double)c[t] / nc) : 0.f;
 }
 
-void launch_centroid_delta(const float* C, int k, int m, float* cprev, float* delta, cudaStream_t s) {
-    k_centroid_delta<<<k, 256, 0, s>>>(C, m, cprev, delta);
+void launch_centroid_delta(const float* C, int k, int m, float* cprev, float* delta, cudaStream_t s, float* craw,
+                           uint8_t* same) {
+    k_centroid_delta<<<k, 256, 0, s>>>(C, m, cprev, delta, craw, same);
     TC_CHECK_LAUNCH();
 }
 

@@ -559,7 +559,8 @@ __global__ void k_permute_bf16(const __nv_bfloat16* __restrict__ xb, const float
 __global__ void __launch_bounds__(128) k_tile_masks(const int32_t* __restrict__ perm, const float* __restrict__ lb,
                                                     const float* __restrict__ ubd, const int32_t* __restrict__ jb,
                                                     const float* __restrict__ delta, float D, int64_t n, int k,
-                                                    unsigned long long* __restrict__ tmask) {
+                                                    unsigned long long* __restrict__ tmask,
+                                                    unsigned long long* __restrict__ series_pairs) {
     __shared__ unsigned long long part[4];
     const int64_t pos = (int64_t)blockIdx.x * 128 + threadIdx.x;
     unsigned long long mask = 0;
@@ -592,6 +593,10 @@ __global__ void __launch_bounds__(128) k_tile_masks(const int32_t* __restrict__ 
         } else {
             for (int j = 0; j < k; ++j) test(j, lr[j]);
         }
+    }
+    if (series_pairs) {  // the pairs the series themselves need (what a per-series pass would evaluate)
+        const unsigned c = __reduce_add_sync(0xffffffffu, (unsigned)__popcll((long long)mask));
+        if ((threadIdx.x & 31) == 0 && c) atomicAdd(series_pairs, (unsigned long long)c);
     }
     const unsigned lo = __reduce_or_sync(0xffffffffu, (unsigned)mask);
     const unsigned hi = __reduce_or_sync(0xffffffffu, (unsigned)(mask >> 32));
@@ -639,11 +644,12 @@ void launch_tile_group(tc_ctx* ctx, int64_t n, int m, int k, const int32_t* gkey
 }
 
 void launch_tile_masks(tc_ctx* ctx, int64_t n, int m, int k, const float* lb, const float* ubd, const int32_t* jb,
-                       const float* delta, float D, TileBounds& out, cudaStream_t s) {
+                       const float* delta, float D, TileBounds& out, cudaStream_t s,
+                       unsigned long long* series_pairs) {
     out = tile_layout(ctx, n, m, k);
     const int64_t ntiles = (n + AT_TILE - 1) / AT_TILE;
     k_tile_masks<<<(unsigned)ntiles, 128, 0, s>>>(out.perm, lb, ubd, jb, delta, D, n, k,
-                                                  const_cast<unsigned long long*>(out.tmask));
+                                                  const_cast<unsigned long long*>(out.tmask), series_pairs);
     TC_CHECK_LAUNCH();
 }
 

@@ -146,6 +146,7 @@ struct Workspace {
     DevBuf bperm;        // n i32 positions -> series, + 2k i32 group counts and cursors
     DevBuf xbfp;         // n x mp bf16 + n f32: the BF16 series and norms in position order
     DevBuf tmask;        // one u64 centroid mask per 128-row tile
+    DevBuf fprev;        // FP32 form with bounds: n f32 + n i32 (label and distance left) + k x m raw centroids + k u8
     DevBuf memo_labels;  // n i32: the labels of the previous extraction (memo of unchanged clusters)
     DevBuf memo_c;       // 3 x k x m f32: that extraction's input and output centroids, this one's input
     DevBuf memo_flags;   // 3k u8 (dirty, skip, gate for the shift pass) + an i32 valid word
@@ -176,8 +177,9 @@ struct BoundsState {
     // bounded passes since the last full pass: their evaluated fractions' sum, count, minimum
     double sum_f = 0, min_f = 2;
     int passes = 0;
-    // totals for tc_assign_stats
-    uint64_t screened = 0, bounded = 0, bounded_pairs = 0;
+    // totals for tc_assign_stats; series_pairs: the pairs the bounded passes' series
+    // themselves needed (their tiles evaluate bounded_pairs)
+    uint64_t screened = 0, bounded = 0, bounded_pairs = 0, series_pairs = 0;
 };
 
 struct tc_ctx {
@@ -256,12 +258,22 @@ struct AssignArgs {
     const float* xbf_norm;
     const int32_t* perm;
     const unsigned long long* tmask;
+    // FFT pass of the FP32 form with bounds: the label and distance it leaves per
+    // series; with reuse, a series whose only candidate is that label, of a centroid
+    // bitwise unchanged since (same[j]), keeps that distance without a transform
+    float* prev_dist;
+    int32_t* prev_label;
+    const uint8_t* same;
+    int reuse;
 };
 void launch_assign_fft(tc_ctx* ctx, const AssignArgs& a, cudaStream_t s);
 // movement of every centroid since cprev (unit vectors, k x m), then cprev <- the unit
 // centroids; delta[j] is rounded up, and +inf where one of the two is zero and the
 // other not
-void launch_centroid_delta(const float* C, int k, int m, float* cprev, float* delta, cudaStream_t s);
+// With craw (k x m, the raw centroids of the previous call): same[j] = centroid j is
+// bitwise unchanged, and craw <- C.
+void launch_centroid_delta(const float* C, int k, int m, float* cprev, float* delta, cudaStream_t s,
+                           float* craw = nullptr, uint8_t* same = nullptr);
 // worst-case |d32 - d| of the FP32 FFT correlation for unit-norm series and centroids
 double fft_error(int m, int F);
 // worst-case |d16 - d32| of the BF16 tensor-core correlation (the screen's half-width)
@@ -294,8 +306,10 @@ struct TileBounds {
 // their BF16 rows in that order; the grouping is kept until the next full pass
 void launch_tile_group(tc_ctx* ctx, int64_t n, int m, int k, const int32_t* gkey, cudaStream_t s);
 // before a bounded pass: the centroid mask of every tile of the kept grouping
+// (series_pairs, if set, accumulates the pairs the series' own masks hold)
 void launch_tile_masks(tc_ctx* ctx, int64_t n, int m, int k, const float* lb, const float* ubd, const int32_t* jb,
-                       const float* delta, float D, TileBounds& out, cudaStream_t s);
+                       const float* delta, float D, TileBounds& out, cudaStream_t s,
+                       unsigned long long* series_pairs = nullptr);
 
 // extraction
 struct ExtractArgs {

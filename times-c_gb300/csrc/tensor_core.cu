@@ -36,7 +36,7 @@ constexpr int GT_PAD = 64;                          // cluster K padding (elemen
 template <int FMT>
 struct GtCfg {
     static constexpr int TILES = FMT == 3 ? 4 : 2;  // operand tiles per stage
-    static constexpr int STAGES = FMT == 3 ? 3 : 4;
+    static constexpr int STAGES = FMT == 3 ? 3 : 6;  // 192 KB of operand ring in flight either way
     static constexpr int SMEM = STAGES * TILES * GT_TILE_BYTES + 1024;  // + alignment slack
     static constexpr int KE = FMT == 1 ? 64 : 32;   // K elements per 128-byte slab
 };
