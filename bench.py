@@ -547,7 +547,7 @@ def run_batched(args):
                    "h2d_bytes_per_step": int(sum(4 * n * m for n, m, k in sizes)),
                    "d2h_bytes_per_step": int(sum(4 * n + 4 * k * m for n, m, k in sizes)),
                    "call": "tc_pool_run_batch (host buffers in, labels/centroids out)"}}
-    print(json.dumps(out), flush=True)
+    return out
 
 
 def run_serving(args):
@@ -575,9 +575,13 @@ def run_serving(args):
     # warm-up, then capacity: a saturated batch with the request mix
     for _ in range(max(1, args.warmup - 2)):
         pool.run_batch([spec_for(k) for k in pick[:8]])
+    # saturated, in arrival order (first in, first out, as the served requests are taken)
     cap_keys = pick[: min(64, len(pick))]
+    cap_specs = [spec_for(k) for k in cap_keys]
     t0 = time.perf_counter()
-    pool.run_batch([spec_for(k) for k in cap_keys])
+    cap_tickets = [pool.submit(sp) for sp in cap_specs]
+    for t in cap_tickets:
+        pool.wait(t)
     capacity = len(cap_keys) / (time.perf_counter() - t0)
     rate = 0.8 * capacity
     gaps = rng.exponential(1.0 / rate, len(pick))
@@ -629,7 +633,26 @@ def run_serving(args):
                    "h2d_bytes_per_step": int(sum(4 * sp.job.n * sp.job.m for sp in specs)),
                    "d2h_bytes_per_step": int(sum(4 * sp.job.n + 4 * sp.job.k * sp.job.m for sp in specs)),
                    "call": "tc_pool_submit / tc_pool_wait"}}
-    print(json.dumps(out), flush=True)
+    return out
+
+
+def many_jobs_samples(args):
+    """The batched and serving forms on bounded samples (128 jobs each), recorded in the
+    default line beside the single-job figures: their own lines come from
+    --workload c4 / c5 (512 jobs).  A failure here is recorded, not raised."""
+    import copy
+    res = {}
+    for name, fn, prec in (("batched", run_batched, "fp32"), ("serving", run_serving, "bf16")):
+        a = copy.copy(args)
+        a.jobs, a.workers, a.max_iter, a.precision, a.steps = 128, 8, 10, prec, 1
+        try:
+            line = fn(a)
+            keep = ("metric", "value", "unit", "ms_per_step", "config", "latency_s", "queue_s", "pairs_per_s",
+                    "jobs_per_s", "e2e", "clocks")
+            res[name] = {key: line[key] for key in keep if key in line}
+        except Exception as e:  # noqa: BLE001 - recorded in the line
+            res[name] = {"error": "%s: %s" % (type(e).__name__, e)}
+    return res
 
 
 def main():
@@ -649,6 +672,8 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-cufft", action="store_true")
+    ap.add_argument("--no-many-jobs", action="store_true",
+                    help="leave out the 128-job samples of the batched and serving forms (c3 line)")
     ap.add_argument("--no-compare", action="store_true",
                     help="leave out the plain FP32 form and dense comparisons (the timed loop is unchanged)")
     args = ap.parse_args()
@@ -656,9 +681,11 @@ def main():
     if args.precision is None:
         args.precision = "bf16" if args.workload in ("c3", "c3s", "c5") else "fp32"
     if args.workload == "c4":
-        return run_batched(args)
+        print(json.dumps(run_batched(args)), flush=True)
+        return
     if args.workload == "c5":
-        return run_serving(args)
+        print(json.dumps(run_serving(args)), flush=True)
+        return
     wl = WORKLOADS[args.workload]
     if args.impl == "reference":
         return run_reference(args, wl)
@@ -872,9 +899,11 @@ def main():
     if out is not None and not args.no_cpu:
         out["cpu_baseline"], out["fp64_oracle_report"] = oracle_iteration_report(ctx, data, x, labels, C, n, m, k,
                                                                                  mode, F, prec)
+    ctx.close()
+    if out is not None and world == 1 and args.workload == "c3" and not args.no_many_jobs:
+        out["many_jobs"] = many_jobs_samples(args)
     if out is not None:
         print(json.dumps(out))
-    ctx.close()
     if dist:
         dist.destroy_process_group()
 

@@ -1,12 +1,12 @@
 """The tensor-core Gram with its K range split across CTAs (shares summed in a fixed
-order) against the unsplit launch (TIMESC_GRAM_NOSPLIT) and the FP64 oracle.
+order) against one share per strip (TIMESC_GRAM_NOSPLIT) and the FP64 oracle.
 
-The split is chosen from the launch's wave occupancy when every share keeps at least
-128 K blocks on average: both cases (m = 512, k = 2, n = 40000 and m = 300, k = 3,
-n = 60000) take 4 shares in FP32 (32-member blocks) and 2 in BF16 (64-member blocks).
-A different summation order moves the Gram by rounding only: centroids within 2e-5
-(3xTF32) / 1e-4 (BF16) of the unsplit ones, and the FP32 form within 1e-4 of the
-oracle.
+Every strip of w column tiles runs as w * base shares (base from the launch's wave
+occupancy, each share keeping at least 64 K blocks on average).  A different
+summation order moves the Gram by rounding only: centroids within 2e-5 (3xTF32) /
+1e-4 (BF16) of the one-share launch, and the FP32 form within 1e-4 of the oracle.
+Cases: m = 512, k = 2, n = 40000 (one diagonal strip of 4 tiles and its neighbours)
+and m = 300, k = 3, n = 60000 (3 row tiles, a partial last tile).
 """
 import numpy as np
 import pytest

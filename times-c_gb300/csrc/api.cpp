@@ -491,7 +491,8 @@ static const char* const WS_NAMES[] = {"x", "labels", "old_labels", "shift", "di
                                        "seg", "perm", "chunk_counts", "counts", "offsets", "gate", "scal",
                                        "gram", "rowsum", "gram_yt", "gram_poff", "piter", "pstats", "aux",
                                        "toeplitz", "toeplitz_norm", "xbf", "xbf_norm", "first", "gram_sq", "sq_meta", "screen", "gram_part",
-                                       "bounds", "cprev", "bstate", "bperm", "xbfp", "tmask"};
+                                       "bounds", "cprev", "bstate", "bperm", "xbfp", "tmask", "memo_labels", "memo_c",
+                                       "memo_flags", "memo_count", "fprev"};
 
 static std::vector<DevBuf*> workspace_buffers(tc_ctx* ctx);
 
@@ -529,7 +530,7 @@ static std::vector<DevBuf*> workspace_buffers(tc_ctx* ctx) {
             &w.gram, &w.rowsum,  &w.gram_yt,    &w.gram_poff, &w.piter,   &w.pstats,    &w.aux,
             &w.toeplitz, &w.toeplitz_norm, &w.xbf, &w.xbf_norm, &w.first, &w.gram_sq, &w.sq_meta, &w.screen, &w.gram_part,
             &w.bounds, &w.cprev, &w.bstate, &w.bperm, &w.xbfp, &w.tmask, &w.memo_labels, &w.memo_c,
-            &w.memo_flags, &w.memo_count};
+            &w.memo_flags, &w.memo_count, &w.fprev};
 }
 
 void release_workspace(tc_ctx* ctx) {

@@ -189,7 +189,7 @@ uint64_t tc_job_footprint(const tc_job* j) {
     b += n * m * 4;                        // members in cluster order
     b += n * 4 * 5;                        // labels, old labels, shifts, distances, permutation
     b += k * m * 4 + k * (F / 2 + 1) * 8;  // centroids, spectra
-    b += 6 * k * m * ld * 4;               // Gram matrices, their K-share partials (<= 4), squares
+    b += 10 * k * m * ld * 4;              // Gram matrices, their K-share partials (<= 8), squares
     b += (k * m + k) * 8 + 3 * k * m * 4;  // row sums, power-iteration vectors
     b += k * 8 * 4;                        // counts, offsets, padded offsets, gates
     const uint64_t esize = j->precision == TC_PREC_BF16 ? 2 : 4;
@@ -203,12 +203,17 @@ uint64_t tc_job_footprint(const tc_job* j) {
         b += n * mp * 2 + n * 4;           // BF16 series and norms
         b += k * (F / 8) * (mp + 56) * 2 + k * 4;  // shifted centroid buffers
     }
-    if (screened) b += n * (tc::SCREEN_CAP + 1) * 4 + k * n * 4 + (k * m + k) * 4;  // candidates, bounds
-    if (j->precision == TC_PREC_BF16 && tc::tc_assign_supported(j->m, (int)F, j->k, j->precision) && k <= 64) {
+    if (screened) b += n * (tc::SCREEN_CAP + 1) * 4;  // candidates
+    const bool bounded = k >= 2 && k <= 64 &&
+                         (screened || (j->precision != TC_PREC_FP32 &&
+                                       tc::tc_assign_supported(j->m, (int)F, j->k, j->precision)));
+    if (bounded) {
         const uint64_t mp = (m + 63) / 64 * 64;
-        b += k * n * 4 + (k * m + k) * 4 + n * 12 + 2 * k * 4;  // bounds, best bounds, grouping
-        b += n * mp * 2 + n * 4 + ((n + 127) / 128) * 8;        // grouped BF16 copy, tile masks
+        b += k * n * 4 + (k * m + k) * 4 + n * 12 + (n + 2 * k * k) * 4;  // bounds, best bounds, grouping
+        b += n * mp * 2 + n * 4 + ((n + 127) / 128) * 8;                  // grouped BF16 copy, tile masks
+        if (screened) b += n * 8 + k * m * 4 + k;                          // FP32 labels, distances, centroids
     }
+    b += n * 4 + 3 * k * m * 4 + 3 * k + 64;  // extraction memo
     b += ((n + 4095) / 4096) * k * 4;      // segment chunk counts
     return b + (1u << 20);
 }

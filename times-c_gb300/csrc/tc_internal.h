@@ -131,7 +131,7 @@ struct Workspace {
     DevBuf rowsum;       // k*m f64 + k f64
     DevBuf piter;        // power-by-squaring vectors 2*k*ld f32
     DevBuf gram_sq;      // k*m*ld f32: squares of the power-by-squaring matrices
-    DevBuf gram_part;    // up to 4 x k*m*ld f32: the Gram's K-share partials
+    DevBuf gram_part;    // up to 8 x k*m*ld f32: the Gram's K-share partials
     DevBuf sq_meta;      // k int64 padded offsets + 2k int32 (column counts, flags)
     DevBuf pstats;       // 3*k*4 f64
     DevBuf aux;          // small scalars (changed count, dist sum, sum_class, flags)

@@ -33,13 +33,57 @@ constexpr int GT_PAD = 64;                          // cluster K padding (elemen
 // FMT 1 = BF16, 2 = TF32, 3 = 3xTF32: x = hi + lo with hi, lo TF32, and
 // S = hi*hi + hi*lo + lo*hi (the dropped lo*lo is below FP32 rounding), FP32-class
 // products on the tensor cores for the plain FP32 form.
+//
+// A CTA computes a strip of one row tile: 128 rows (tile r) against w column tiles,
+// one 128-column TMEM accumulator each, so every operand tile it loads serves w
+// products (a 128 x 128 tile per CTA loads two tiles per product).  A strip that
+// starts at the diagonal (q0 = r) holds up to W0 tiles and its A is its first B
+// tile; the rest of the row goes in strips of up to W0 - 1 tiles plus the A tile.
+// At m = 512 (4 row tiles, BF16) that is 4 strips of 4, 3, 2, 1 tiles: 10 tile loads
+// per K slab of a cluster against 16 for tile pairs.  A strip of w tiles is split
+// into w * base shares of its K range, so every CTA does the same work (its share's
+// K blocks times w products); the shares' partials are summed in a fixed order.
 template <int FMT>
 struct GtCfg {
-    static constexpr int TILES = FMT == 3 ? 4 : 2;  // operand tiles per stage
-    static constexpr int STAGES = FMT == 3 ? 3 : 6;  // 192 KB of operand ring in flight either way
-    static constexpr int SMEM = STAGES * TILES * GT_TILE_BYTES + 1024;  // + alignment slack
+    static constexpr int PLANES = FMT == 3 ? 2 : 1;   // hi and lo planes (3xTF32)
+    static constexpr int W0 = FMT == 3 ? 2 : 4;        // tiles per stage and plane
+    static constexpr int STAGES = 3;
+    static constexpr int STAGE_BYTES = W0 * PLANES * GT_TILE_BYTES;  // 64 KB
+    static constexpr int SMEM = STAGES * STAGE_BYTES + 1024;         // + alignment slack
+    static constexpr int TMEM_COLS = W0 * 128;                        // a power of two
     static constexpr int KE = FMT == 1 ? 64 : 32;   // K elements per 128-byte slab
 };
+
+// Strips of the upper triangle of nt x nt tiles, row by row (widest first in each row).
+__host__ __device__ inline int gram_row_strips(int nt, int r, int w0) {
+    const int rest = nt - r - w0;
+    return 1 + (rest > 0 ? (rest + w0 - 2) / (w0 - 1) : 0);
+}
+__host__ __device__ inline int gram_strips(int nt, int w0) {
+    int s = 0;
+    for (int r = 0; r < nt; ++r) s += gram_row_strips(nt, r, w0);
+    return s;
+}
+// strip t -> row tile r, first column tile q0, width w, diagonal (A is B tile 0)
+__host__ __device__ inline void gram_strip(int nt, int w0, int t, int& r, int& q0, int& w, bool& diag) {
+    r = 0;
+    while (t >= gram_row_strips(nt, r, w0)) t -= gram_row_strips(nt, r++, w0);
+    if (t == 0) {
+        q0 = r;
+        w = nt - r < w0 ? nt - r : w0;
+        diag = true;
+    } else {
+        q0 = r + w0 + (t - 1) * (w0 - 1);
+        w = nt - q0 < w0 - 1 ? nt - q0 : w0 - 1;
+        diag = false;
+    }
+}
+// width of the strip holding tile (lo, hi), lo <= hi
+__host__ __device__ inline int gram_strip_width(int nt, int w0, int lo, int hi) {
+    if (hi < lo + w0) return nt - lo < w0 ? nt - lo : w0;
+    const int q0 = lo + w0 + (hi - lo - w0) / (w0 - 1) * (w0 - 1);
+    return nt - q0 < w0 - 1 ? nt - q0 : w0 - 1;
+}
 
 // ---------------------------------------------------------------- TMA descriptor
 typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
@@ -141,13 +185,16 @@ __global__ void __launch_bounds__(128, 1) k_gram_tc(const __grid_constant__ CUte
     const int c = blockIdx.y;
     const int cnt = counts[c];
     if (cnt == 0 || (skip && skip[c])) return;
-    int t = blockIdx.x, ta = 0;
-    while (t >= nt - ta) { t -= nt - ta; ++ta; }
-    const int tb = ta + t;
+    int r, q0, w;
+    bool diag;
+    gram_strip(nt, G::W0, blockIdx.x, r, q0, w, diag);
+    const int ns = nsplit > 0 ? w * nsplit : 1, z = blockIdx.z;  // this strip's shares (0: one)
+    if (z >= ns) return;
+    const int nload = diag ? w : w + 1;  // operand tiles per stage and plane
     constexpr int KE = G::KE;
-    // split K: this CTA's share of the cluster's K blocks, into partial buffer z
-    const int nk_all = (cnt + KE - 1) / KE, z = blockIdx.z;
-    const int kb0 = (int)((int64_t)z * nk_all / nsplit), nk = (int)((int64_t)(z + 1) * nk_all / nsplit) - kb0;
+    // this CTA's share of the cluster's K blocks, into partial buffer z
+    const int nk_all = (cnt + KE - 1) / KE;
+    const int kb0 = (int)((int64_t)z * nk_all / ns), nk = (int)((int64_t)(z + 1) * nk_all / ns) - kb0;
     if (nk == 0) return;  // the sum kernel skips empty shares
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     if (threadIdx.x == 0) {
@@ -161,7 +208,7 @@ __global__ void __launch_bounds__(128, 1) k_gram_tc(const __grid_constant__ CUte
         if (FMT == 3) sm100::prefetch_tmap(&tmap_lo);
     }
     if (warp == 0) {
-        sm100::tmem_alloc(&tmem_base, 128);
+        sm100::tmem_alloc(&tmem_base, G::TMEM_COLS);
         sm100::tmem_relinquish();
     }
     sm100::tc_fence_before();
@@ -169,6 +216,10 @@ __global__ void __launch_bounds__(128, 1) k_gram_tc(const __grid_constant__ CUte
     sm100::tc_fence_after();
     const uint32_t tmem = tmem_base;
     const int x0 = (int)poff[c];
+    // stage layout: [plane][slot] tiles of 16 KB; slot 0 = A (= B tile 0 on the diagonal)
+    auto slot_ptr = [&](uint8_t* st, int plane, int slot) {
+        return st + (size_t)(plane * G::W0 + slot) * GT_TILE_BYTES;
+    };
     bool ok = true;
     if (warp == 0 && lane == 0) {
         // TMA producer
@@ -176,15 +227,13 @@ __global__ void __launch_bounds__(128, 1) k_gram_tc(const __grid_constant__ CUte
             const int s = kb % G::STAGES, u = kb / G::STAGES;
             if (u > 0) ok = sm100::mbar_wait(&empty[s], (u - 1) & 1, err);
             if (!ok) break;
-            uint8_t* A = base + (size_t)s * G::TILES * GT_TILE_BYTES;  // [A | B | A_lo | B_lo]
-            // a diagonal tile's B is its A: loaded once
-            sm100::mbar_expect_tx(&full[s], (ta == tb ? G::TILES / 2 : G::TILES) * GT_TILE_BYTES);
+            uint8_t* st = base + (size_t)s * G::STAGE_BYTES;
+            sm100::mbar_expect_tx(&full[s], (uint32_t)(nload * G::PLANES * GT_TILE_BYTES));
             const int xk = x0 + (kb0 + kb) * KE;
-            sm100::tma_load_2d(A, &tmap, xk, ta * GT_TILE, &full[s]);
-            if (ta != tb) sm100::tma_load_2d(A + GT_TILE_BYTES, &tmap, xk, tb * GT_TILE, &full[s]);
-            if (FMT == 3) {
-                sm100::tma_load_2d(A + 2 * GT_TILE_BYTES, &tmap_lo, xk, ta * GT_TILE, &full[s]);
-                if (ta != tb) sm100::tma_load_2d(A + 3 * GT_TILE_BYTES, &tmap_lo, xk, tb * GT_TILE, &full[s]);
+            for (int l = 0; l < nload; ++l) {
+                const int tile = diag ? q0 + l : (l == 0 ? r : q0 + l - 1);
+                sm100::tma_load_2d(slot_ptr(st, 0, l), &tmap, xk, tile * GT_TILE, &full[s]);
+                if (FMT == 3) sm100::tma_load_2d(slot_ptr(st, 1, l), &tmap_lo, xk, tile * GT_TILE, &full[s]);
             }
         }
         // the MMA thread's last commits to empty[] arrive when their MMAs end: wait for
@@ -194,27 +243,31 @@ __global__ void __launch_bounds__(128, 1) k_gram_tc(const __grid_constant__ CUte
             for (int kb = nk > G::STAGES ? nk - G::STAGES : 0; kb < nk; ++kb)
                 sm100::mbar_wait(&empty[kb % G::STAGES], (kb / G::STAGES) & 1, err);
     } else if (warp == 1 && lane == 0) {
-        // MMA issuer
+        // MMA issuer: one 128 x 128 accumulator per column tile of the strip
         constexpr uint32_t ID = sm100::idesc(FMT == 1 ? 1 : 2, 128, 128);
         for (int kb = 0; kb < nk && ok; ++kb) {
             const int s = kb % G::STAGES, u = kb / G::STAGES;
             ok = sm100::mbar_wait(&full[s], u & 1, err);
             if (!ok) break;
             sm100::tc_fence_after();
-            uint8_t* A = base + (size_t)s * G::TILES * GT_TILE_BYTES;
-            const int bo = ta == tb ? 0 : GT_TILE_BYTES;  // a diagonal tile's B is its A
-            const uint64_t da = sm100::desc_k_sw128(A), db = sm100::desc_k_sw128(A + bo);
+            uint8_t* st = base + (size_t)s * G::STAGE_BYTES;
+            const uint64_t da = sm100::desc_k_sw128(slot_ptr(st, 0, 0));
+            const uint64_t dal = FMT == 3 ? sm100::desc_k_sw128(slot_ptr(st, 1, 0)) : 0;
+            for (int i = 0; i < w; ++i) {
+                const int bs = diag ? i : i + 1;
+                const uint64_t db = sm100::desc_k_sw128(slot_ptr(st, 0, bs));
+                const uint32_t acc = tmem + (uint32_t)(i * 128);
 #pragma unroll
-            for (int kk = 0; kk < 4; ++kk) {  // 4 x 32 bytes of K per slab
-                if (FMT == 1) {
-                    sm100::mma_f16(tmem, da + 2 * kk, db + 2 * kk, ID, (kb | kk) != 0);
-                } else {
-                    sm100::mma_tf32(tmem, da + 2 * kk, db + 2 * kk, ID, (kb | kk) != 0);
-                    if (FMT == 3) {
-                        const uint64_t dal = sm100::desc_k_sw128(A + 2 * GT_TILE_BYTES);
-                        const uint64_t dbl = sm100::desc_k_sw128(A + 2 * GT_TILE_BYTES + bo);
-                        sm100::mma_tf32(tmem, da + 2 * kk, dbl + 2 * kk, ID, 1);
-                        sm100::mma_tf32(tmem, dal + 2 * kk, db + 2 * kk, ID, 1);
+                for (int kk = 0; kk < 4; ++kk) {  // 4 x 32 bytes of K per slab
+                    if (FMT == 1) {
+                        sm100::mma_f16(acc, da + 2 * kk, db + 2 * kk, ID, (kb | kk) != 0);
+                    } else {
+                        sm100::mma_tf32(acc, da + 2 * kk, db + 2 * kk, ID, (kb | kk) != 0);
+                        if (FMT == 3) {
+                            const uint64_t dbl = sm100::desc_k_sw128(slot_ptr(st, 1, bs));
+                            sm100::mma_tf32(acc, da + 2 * kk, dbl + 2 * kk, ID, 1);
+                            sm100::mma_tf32(acc, dal + 2 * kk, db + 2 * kk, ID, 1);
+                        }
                     }
                 }
             }
@@ -223,27 +276,30 @@ __global__ void __launch_bounds__(128, 1) k_gram_tc(const __grid_constant__ CUte
         sm100::mma_commit(&done);
     }
     __syncwarp();
-    // epilogue: warp w owns TMEM lanes 32w..32w+31 = rows a0 + 32w + lane
+    // epilogue: warp w owns TMEM lanes 32w..32w+31 = rows r*128 + 32w + lane
     const bool fin = __syncthreads_and(sm100::mbar_wait(&done, 0, err)) != 0;
     sm100::tc_fence_after();
     if (fin) {
-        const int a = ta * GT_TILE + warp * 32 + lane;
+        const int a = r * GT_TILE + warp * 32 + lane;
         float* Sc = S + (size_t)z * part_stride + (size_t)c * m * ld;
-        for (int cb = 0; cb < 4; ++cb) {
-            float r[32];
-            sm100::tmem_ld32(tmem + ((uint32_t)(warp * 32) << 16) + cb * 32, r);
-            sm100::tmem_ld_wait();
-            const int b0 = tb * GT_TILE + cb * 32;
-            if (a < m) {  // the row's 32 values as float4 (columns m..ld-1 are products with zero rows: 0)
-                float4* row4 = reinterpret_cast<float4*>(Sc + (size_t)a * ld + b0);
+        for (int i = 0; i < w; ++i) {
+            const int q = q0 + i;
+            for (int cb = 0; cb < 4; ++cb) {
+                float v[32];
+                sm100::tmem_ld32(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(i * 128 + cb * 32), v);
+                sm100::tmem_ld_wait();
+                const int b0 = q * GT_TILE + cb * 32;
+                if (a < m) {  // the row's 32 values as float4 (columns m..ld-1 are products with zero rows: 0)
+                    float4* row4 = reinterpret_cast<float4*>(Sc + (size_t)a * ld + b0);
 #pragma unroll
-                for (int q = 0; q < 8; ++q)
-                    if (b0 + 4 * q < ld) row4[q] = make_float4(r[4 * q], r[4 * q + 1], r[4 * q + 2], r[4 * q + 3]);
-            }
-            if (ta != tb) {
+                    for (int e = 0; e < 8; ++e)
+                        if (b0 + 4 * e < ld) row4[e] = make_float4(v[4 * e], v[4 * e + 1], v[4 * e + 2], v[4 * e + 3]);
+                }
+                if (q != r) {  // the mirror image below the diagonal
 #pragma unroll
-                for (int j = 0; j < 32; ++j)
-                    if (b0 + j < m && a < m) Sc[(size_t)(b0 + j) * ld + a] = r[j];
+                    for (int e = 0; e < 32; ++e)
+                        if (b0 + e < m && a < m) Sc[(size_t)(b0 + e) * ld + a] = v[e];
+                }
             }
         }
     } else if (threadIdx.x == 0) {
@@ -252,26 +308,31 @@ __global__ void __launch_bounds__(128, 1) k_gram_tc(const __grid_constant__ CUte
     }
     sm100::tc_fence_before();
     __syncthreads();
-    if (warp == 0) sm100::tmem_dealloc(tmem, 128);
+    if (warp == 0) sm100::tmem_dealloc(tmem, G::TMEM_COLS);
 }
 
-// S_c = sum of the K shares' partial Grams, in share order (deterministic); shares
-// with no K blocks wrote nothing and are skipped.  Rows a < m, columns < ld (the
-// padding columns are zeros in every partial).
-__global__ void k_gram_sum(const float* __restrict__ P, int nsplit, size_t part_stride,
+// S_c = sum of the K shares' partial Grams, in share order (deterministic): the
+// region of tile (lo, hi) comes from the strip holding it, split in width * base
+// shares; shares with no K blocks wrote nothing and are skipped.  Rows a < m,
+// columns < ld (the padding columns are zeros in every partial).
+__global__ void k_gram_sum(const float* __restrict__ P, int base, int w0, int nt, size_t part_stride,
                            const int32_t* __restrict__ counts, int KE, int m, int ld, float* __restrict__ S,
                            const uint8_t* __restrict__ skip) {
     const int c = blockIdx.y;
     const int cnt = counts[c];
     if (cnt == 0 || (skip && skip[c])) return;
     const int nk = (cnt + KE - 1) / KE;
-    const size_t n4 = (size_t)m * ld / 4, off = (size_t)c * m * ld / 4;
+    const int ld4 = ld / 4;
+    const size_t n4 = (size_t)m * ld4, off = (size_t)c * m * ld / 4;
     const float4* P4 = reinterpret_cast<const float4*>(P);
     float4* S4 = reinterpret_cast<float4*>(S);
     for (size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x; e < n4; e += (size_t)gridDim.x * blockDim.x) {
+        const int ta = (int)(e / ld4) / GT_TILE;
+        const int tb = min((int)(e % ld4) * 4 / GT_TILE, nt - 1);
+        const int ns = base > 0 ? gram_strip_width(nt, w0, min(ta, tb), max(ta, tb)) * base : 1;
         float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
-        for (int z = 0; z < nsplit; ++z) {
-            if ((int64_t)(z + 1) * nk / nsplit == (int64_t)z * nk / nsplit) continue;
+        for (int z = 0; z < ns; ++z) {
+            if ((int64_t)(z + 1) * nk / ns == (int64_t)z * nk / ns) continue;
             const float4 q = P4[z * (part_stride / 4) + off + e];
             v.x += q.x;
             v.y += q.y;
@@ -360,25 +421,30 @@ void launch_gram_tc(tc_ctx* ctx, const float* seg, const int32_t* counts, const 
     CUtensorMap map = make_tmap_2d(YT, dt, esize, (uint64_t)m, (uint64_t)Pp, GT_TILE);
     CUtensorMap map_lo = fmt == 3 ? make_tmap_2d(YTlo, dt, esize, (uint64_t)m, (uint64_t)Pp, GT_TILE) : map;
     const int nt = ceil_div(m, GT_TILE);
-    // K split across CTAs so the launch fills its last wave (one CTA per SM: the
-    // operand ring takes most of the shared memory): the share count with the best
-    // wave occupancy, each share keeping at least 128 K blocks on average (with fewer,
-    // a CTA's fixed costs - setup, pipeline fill, the tile and mirror stores, its
-    // partial's share of the sum - outweigh the fuller wave)
+    // A strip of w tiles runs as w * base CTAs over shares of its K range, so every
+    // CTA does the same work; base (1..W0 / 2 ... 2 shares per tile product) is the
+    // count that best fills the launch's last wave (one CTA per SM: the operand ring
+    // takes most of the shared memory) while every share keeps at least 64 K blocks of
+    // a tile product on average (with fewer, a CTA's fixed costs - setup, pipeline
+    // fill, the strip and mirror stores, its partial's share of the sum - outweigh the
+    // fuller wave).  The partials are summed in a fixed order.
     const int KE = fmt == 1 ? GtCfg<1>::KE : GtCfg<3>::KE;
-    const int units = nt * (nt + 1) / 2 * k;
+    const int w0 = fmt == 1 ? GtCfg<1>::W0 : (fmt == 2 ? GtCfg<2>::W0 : GtCfg<3>::W0);
+    const int strips = gram_strips(nt, w0);
+    const int units = nt * (nt + 1) / 2 * k;  // CTAs per unit of base: one per tile product
     const int64_t avg_kb = std::max<int64_t>(1, n / std::max(k, 1) / KE);
-    auto occupancy = [&](int sp) {
-        const double x = (double)units * sp / ctx->sm_count;
+    auto occupancy = [&](int b) {
+        const double x = (double)units * b / ctx->sm_count;
         return x / std::ceil(x);
     };
-    int nsplit = 1;
-    for (int sp = 2; sp <= 4 && avg_kb / sp >= 128; ++sp)
-        if (occupancy(sp) > occupancy(nsplit) + 0.02) nsplit = sp;
-    if (std::getenv("TIMESC_GRAM_NOSPLIT")) nsplit = 1;
+    int nsplit = 1;  // base
+    for (int b = 2; b * w0 <= 8 && avg_kb / b >= 64; ++b)
+        if (occupancy(b) > occupancy(nsplit) + 0.02) nsplit = b;
+    if (std::getenv("TIMESC_GRAM_NOSPLIT")) nsplit = 0;  // one share per strip (for comparison)
+    const int shares = nsplit > 0 ? w0 * nsplit : 1;
     const size_t part_stride = (size_t)k * m * ld;
-    float* out = nsplit > 1 ? ctx->ws.gram_part.as<float>((size_t)nsplit * part_stride) : S;
-    dim3 grid(nt * (nt + 1) / 2, k, nsplit);
+    float* out = ctx->ws.gram_part.as<float>((size_t)shares * part_stride);
+    dim3 grid(strips, k, shares);
     if (fmt == 1) {
         allow_max_dynamic_smem(k_gram_tc<1>);
         k_gram_tc<1><<<grid, 128, GtCfg<1>::SMEM, s>>>(map, map_lo, counts, poff, m, ld, nt, nsplit, part_stride,
@@ -393,11 +459,9 @@ void launch_gram_tc(tc_ctx* ctx, const float* seg, const int32_t* counts, const 
                                                         out, err, skip);
     }
     TC_CHECK_LAUNCH();
-    if (nsplit > 1) {
-        k_gram_sum<<<dim3(ceil_div((int64_t)m * ld / 4, 256 * 4), k), 256, 0, s>>>(out, nsplit, part_stride, counts,
-                                                                                  KE, m, ld, S, skip);
-        TC_CHECK_LAUNCH();
-    }
+    k_gram_sum<<<dim3(ceil_div((int64_t)m * ld / 4, 256 * 4), k), 256, 0, s>>>(out, nsplit, w0, nt, part_stride,
+                                                                              counts, KE, m, ld, S, skip);
+    TC_CHECK_LAUNCH();
 }
 
 }  // namespace tc
