@@ -431,9 +431,36 @@ __global__ void __launch_bounds__(AT_THREADS, 1) k_assign_tc(const __grid_consta
                 if (p.tmask) {  // the centroids the tile skipped: bounds carried down
                     float* lr = p.lb_out + (size_t)i * p.k;
                     const unsigned long long all = p.k >= 64 ? ~0ull : ((1ull << p.k) - 1ull);
-                    for (unsigned long long mk = all & ~tmask; mk; mk &= mk - 1) {
-                        const int j = __ffsll((long long)mk) - 1;
-                        lr[j] = __fsub_rd(lr[j], __ldg(p.delta + j));
+                    const unsigned long long skipm = all & ~tmask;
+                    if ((p.k & 3) == 0) {
+                        // the row as float4s (rows are 16-byte aligned), 8 at a time: every
+                        // load of a batch is issued before its updates, instead of one
+                        // dependent read-modify-write per skipped centroid
+                        float4* l4 = reinterpret_cast<float4*>(lr);
+                        const int n4 = p.k >> 2;
+                        for (int b0 = 0; b0 < n4; b0 += 8) {
+                            float4 v[8];
+#pragma unroll
+                            for (int e = 0; e < 8; ++e)
+                                if (b0 + e < n4 && ((skipm >> (4 * (b0 + e))) & 0xFull)) v[e] = l4[b0 + e];
+#pragma unroll
+                            for (int e = 0; e < 8; ++e) {
+                                const int q4 = b0 + e;
+                                const unsigned bits = q4 < n4 ? (unsigned)(skipm >> (4 * q4)) & 0xFu : 0u;
+                                if (!bits) continue;
+                                const float* dl = p.delta + 4 * q4;
+                                if (bits & 1u) v[e].x = __fsub_rd(v[e].x, __ldg(dl));
+                                if (bits & 2u) v[e].y = __fsub_rd(v[e].y, __ldg(dl + 1));
+                                if (bits & 4u) v[e].z = __fsub_rd(v[e].z, __ldg(dl + 2));
+                                if (bits & 8u) v[e].w = __fsub_rd(v[e].w, __ldg(dl + 3));
+                                l4[q4] = v[e];
+                            }
+                        }
+                    } else {
+                        for (unsigned long long mk = skipm; mk; mk &= mk - 1) {
+                            const int j = __ffsll((long long)mk) - 1;
+                            lr[j] = __fsub_rd(lr[j], __ldg(p.delta + j));
+                        }
                     }
                 }
                 if (p.ubd) {
