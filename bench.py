@@ -575,8 +575,10 @@ def run_serving(args):
     # warm-up, then capacity: a saturated batch with the request mix
     for _ in range(max(1, args.warmup - 2)):
         pool.run_batch([spec_for(k) for k in pick[:8]])
-    # saturated, in arrival order (first in, first out, as the served requests are taken)
-    cap_keys = pick[: min(64, len(pick))]
+    # saturated, in arrival order (first in, first out, as the served requests are taken),
+    # on the first quarter of the request list (at least 64) so that its share of large
+    # requests is close to the whole run's
+    cap_keys = pick[: min(max(64, len(pick) // 4), len(pick))]
     cap_specs = [spec_for(k) for k in cap_keys]
     t0 = time.perf_counter()
     cap_tickets = [pool.submit(sp) for sp in cap_specs]
