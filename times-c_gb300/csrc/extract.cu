@@ -354,7 +354,7 @@ struct MemoBuffers {
     unsigned long long* count;
 };
 
-static MemoBuffers memo_buffers(tc_ctx* ctx, int64_t n, int k, int m) {
+static MemoBuffers memo_buffers(tc_ctx* ctx, int64_t n, int k, int m, cudaStream_t s) {
     Workspace& ws = ctx->ws;
     MemoBuffers b;
     b.labels = ws.memo_labels.as<int32_t>(std::max<int64_t>(n, 1));
@@ -370,7 +370,7 @@ static MemoBuffers memo_buffers(tc_ctx* ctx, int64_t n, int k, int m) {
     b.valid = reinterpret_cast<int*>(f + fb);
     if (!ctx->memo.counters || !ws.memo_count.p) {  // outside graph capture (memo_prepare comes first)
         b.count = ws.memo_count.as<unsigned long long>(3);
-        TC_CUDA(cudaMemset(b.count, 0, 3 * sizeof(unsigned long long)));
+        TC_CUDA(cudaMemsetAsync(b.count, 0, 3 * sizeof(unsigned long long), s));
         ctx->memo.counters = true;
     }
     b.count = static_cast<unsigned long long*>(ws.memo_count.p);
@@ -385,7 +385,7 @@ static bool memo_keyed_for(const tc_ctx* ctx, const ExtractArgs& a) {
 
 void memo_prepare(tc_ctx* ctx, const ExtractArgs& a, cudaStream_t s) {
     if (!a.memo || a.n <= 0) return;
-    const MemoBuffers b = memo_buffers(ctx, a.n, a.k, a.m);  // allocated here, before any capture
+    const MemoBuffers b = memo_buffers(ctx, a.n, a.k, a.m, s);  // allocated here, before any capture
     if (memo_keyed_for(ctx, a)) return;
     MemoState& ms = ctx->memo;
     TC_CUDA(cudaMemsetAsync(b.valid, 0, sizeof(int), s));
@@ -460,7 +460,7 @@ void extract_async(tc_ctx* ctx, const ExtractArgs& a, cudaStream_t s) {
     const uint8_t* skip = nullptr;
     const uint8_t* gate_shift = gate;
     if (memo) {
-        mb = memo_buffers(ctx, n, k, m);
+        mb = memo_buffers(ctx, n, k, m, s);
         TC_CUDA(cudaMemsetAsync(mb.dirty, 0, k, s));
         const int g = (int)std::min<int64_t>(ceil_div(n, 256), (int64_t)ctx->sm_count * 8);
         k_memo_dirty<<<g, 256, 0, s>>>(a.labels, mb.labels, n, k, mb.dirty);

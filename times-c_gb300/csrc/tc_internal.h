@@ -94,6 +94,9 @@ struct DevBuf {
             p = static_cast<char*>(p) + g;
             cudaMemset(static_cast<char*>(p) + need, GUARD_BYTE, g);
             cudaMemset(p, 0xFF, need);  // NaN floats, -1 integers: reads before writes show up
+            // cudaMemset runs on the legacy stream, which does not order with the
+            // contexts' non-blocking streams: finish the fills before the buffer is used
+            cudaDeviceSynchronize();
         }
         bytes = need;
         return p;

@@ -21,6 +21,7 @@
 #include <cstdlib>
 #include <vector>
 
+#include "gram_strips.h"
 #include "sm100.cuh"
 #include "tc_internal.h"
 
@@ -53,37 +54,6 @@ struct GtCfg {
     static constexpr int TMEM_COLS = W0 * 128;                        // a power of two
     static constexpr int KE = FMT == 1 ? 64 : 32;   // K elements per 128-byte slab
 };
-
-// Strips of the upper triangle of nt x nt tiles, row by row (widest first in each row).
-__host__ __device__ inline int gram_row_strips(int nt, int r, int w0) {
-    const int rest = nt - r - w0;
-    return 1 + (rest > 0 ? (rest + w0 - 2) / (w0 - 1) : 0);
-}
-__host__ __device__ inline int gram_strips(int nt, int w0) {
-    int s = 0;
-    for (int r = 0; r < nt; ++r) s += gram_row_strips(nt, r, w0);
-    return s;
-}
-// strip t -> row tile r, first column tile q0, width w, diagonal (A is B tile 0)
-__host__ __device__ inline void gram_strip(int nt, int w0, int t, int& r, int& q0, int& w, bool& diag) {
-    r = 0;
-    while (t >= gram_row_strips(nt, r, w0)) t -= gram_row_strips(nt, r++, w0);
-    if (t == 0) {
-        q0 = r;
-        w = nt - r < w0 ? nt - r : w0;
-        diag = true;
-    } else {
-        q0 = r + w0 + (t - 1) * (w0 - 1);
-        w = nt - q0 < w0 - 1 ? nt - q0 : w0 - 1;
-        diag = false;
-    }
-}
-// width of the strip holding tile (lo, hi), lo <= hi
-__host__ __device__ inline int gram_strip_width(int nt, int w0, int lo, int hi) {
-    if (hi < lo + w0) return nt - lo < w0 ? nt - lo : w0;
-    const int q0 = lo + w0 + (hi - lo - w0) / (w0 - 1) * (w0 - 1);
-    return nt - q0 < w0 - 1 ? nt - q0 : w0 - 1;
-}
 
 // ---------------------------------------------------------------- TMA descriptor
 typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
