@@ -199,8 +199,19 @@ typedef struct {
 
 /* The reference's whole path after parsing: copy in (if h_data), z-normalise,
  * initialise, iterate (extract/assign/converge in the reference's loop order for
- * init_chose), apply the restart rule, copy labels/centroids out.  Synchronous. */
+ * init_chose), apply the restart rule, copy labels/centroids out.  Synchronous.
+ * Each iteration's stages are replayed from CUDA graphs.  With TIMESC_DEVICE_LOOP=1
+ * in the environment, once those are captured the remaining iterations run as one
+ * graph launch: a conditional WHILE node over the stages, with the convergence test,
+ * the class-count stop and the assignment's bounds rule evaluated on the device (no
+ * host round trip per iteration; the same results as the host-driven loop). */
 int tc_kshape_run(tc_ctx* ctx, const tc_job* job, tc_result* result);
+
+/* Iterations of tc_kshape_run on this context since its creation that ran inside
+ * the loop graph and on the host, and loop graphs built.  Any output may be NULL.
+ * No counterpart in the reference. */
+int tc_loop_stats(const tc_ctx* ctx, uint64_t* device_iterations, uint64_t* host_iterations,
+                  uint64_t* graphs_built);
 
 /* ---------------------------------------------------------------- many jobs: batch and serving */
 /* No counterpart in the reference, which runs one job per process.  A pool owns

@@ -24,7 +24,8 @@ NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "--expt-r
 CXX_FLAGS = ["-O2", "-std=c++17", "-fPIC", "-pthread", "-I", os.path.join(ROOT, "include"), "-I", CSRC,
              "-I", "/usr/local/cuda/include"]
 
-CU_SOURCES = ["assign_fft.cu", "znorm.cu", "extract.cu", "power.cu", "power_sq.cu", "tensor_core.cu", "assign_tc.cu"]
+CU_SOURCES = ["assign_fft.cu", "znorm.cu", "extract.cu", "power.cu", "power_sq.cu", "tensor_core.cu", "assign_tc.cu",
+              "loop_graph.cu"]
 CPP_SOURCES = ["api.cpp", "io.cpp", "gen.cpp", "pool.cpp"]
 
 

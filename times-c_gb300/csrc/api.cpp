@@ -6,6 +6,7 @@
 #include <cstring>
 #include <new>
 
+#include "loop_graph.h"
 #include "tc_internal.h"
 
 std::recursive_mutex& capture_mutex() {
@@ -67,9 +68,8 @@ static void check_shape(int64_t n, int m, int k, int mode) {
 //     pass is run again once the bounded passes since the last one have cost, beyond
 //     the cheapest of them, about one full pass (in units of a full tensor-core pass:
 //     sum of evaluated fractions - passes x their minimum >= BOUNDS_REFRESH_COST).
-enum { BOUNDS_OFF = 0, BOUNDS_AUTO = -1, BOUNDS_REFRESH = 1, BOUNDS_USE = 2, BOUNDS_USE_REGROUP = 3 };
-constexpr double BOUNDS_REFRESH_COST = 1.0;
-constexpr int64_t BOUNDS_REGROUP_SHARE = 200;
+// (BOUNDS_* modes and the two constants: loop_graph.h, whose control kernels restate
+// the same rule on the device.)
 
 static bool bounded_mode(int use) { return use == BOUNDS_USE || use == BOUNDS_USE_REGROUP; }
 
@@ -279,6 +279,7 @@ static void check_async_errors(const int* words) {
 // the stage keeps issuing its launches directly.
 struct StageGraph {
     cudaGraphExec_t exec = nullptr;
+    cudaGraph_t graph = nullptr;  // kept for the loop graph, which embeds it
     bool warm = false, failed = false;
     uint64_t kernels = 0;  // kernel launches recorded in the graph
     StageGraph() = default;
@@ -286,6 +287,7 @@ struct StageGraph {
     StageGraph& operator=(const StageGraph&) = delete;
     ~StageGraph() {
         if (exec) cudaGraphExecDestroy(exec);
+        if (graph) cudaGraphDestroy(graph);
     }
     template <class F>
     void run(bool enabled, cudaStream_t s, F&& issue) {
@@ -325,7 +327,8 @@ struct StageGraph {
             exec = nullptr;
             failed = true;
         }
-        if (gr) cudaGraphDestroy(gr);
+        if (exec) graph = gr;
+        else if (gr) cudaGraphDestroy(gr);
         cudaGetLastError();
     }
 };
@@ -467,7 +470,123 @@ static LoopState run_loop(tc_ctx* ctx, const tc_job* job, const float* x, int k,
         TC_REQUIRE(h.bad_label == 0, TC_ERR_ARG, "a label is outside [0, k)");
         if (!cal_select) st.sum_class = h.sum_class;  // get_class_centers_a leaves sum_class alone
     };
+    // With TIMESC_DEVICE_LOOP=1: the whole loop as one graph (loop_graph.h) once the
+    // extraction and the assignment variant an iteration needs are captured; until then,
+    // and whenever the graph returns for a variant it does not hold yet, the host runs
+    // the iteration.  Off by default: on a GB300 host the two read-backs an iteration
+    // takes cost a few microseconds, about what the graph's conditional nodes and
+    // control kernels cost, and building the graph (twice per run) cost more than that.
+    const char* dl_env = std::getenv("TIMESC_DEVICE_LOOP");
+    const bool dev_loop = graphs && dl_env && std::strcmp(dl_env, "0") != 0 && !ctx->loop_graph_failed &&
+                          !guard_bytes(1) && !std::getenv("TIMESC_TRACE");
+    StageGraph* variants[3] = {&g_assign, &g_assign_bounded, &g_assign_regroup};
+    struct LoopExec {
+        cudaGraphExec_t exec = nullptr;
+        int avail = -1;  // the variants it holds
+        ~LoopExec() {
+            if (exec) cudaGraphExecDestroy(exec);
+        }
+    } lx;
+    LoopCtl* dctl = dev_loop ? ws.loopctl.as<LoopCtl>(1) : nullptr;
+    // true once the loop has ended on the device; otherwise i is the iteration the host runs
+    auto device_loop = [&](int& i) -> bool {
+        if (!dev_loop || !g_extract.graph) return false;
+        const int mode = bnd ? bounds_mode(ctx->bounds, BOUNDS_AUTO) : BOUNDS_OFF;
+        int avail = 0;
+        for (int v = 0; v < 3; ++v)
+            if (variants[v]->graph) avail |= 1 << v;
+        if (!((avail >> assign_variant(mode)) & 1)) return false;
+        if (lx.avail != avail) {
+            if (lx.exec) cudaGraphExecDestroy(lx.exec);
+            LoopGraphSpec sp;
+            sp.extract = g_extract.graph;
+            for (int v = 0; v < 3; ++v) sp.assign[v] = variants[v]->graph;
+            sp.order_tsl = order_tsl;
+            sp.ctl = dctl;
+            sp.aux = aux;
+            sp.labels = labels;
+            sp.old_labels = old;
+            sp.n = n;
+            lx.exec = build_loop_graph(sp);
+            lx.avail = avail;
+            ++ctx->loop.builds;
+            if (!lx.exec) {
+                ctx->loop_graph_failed = true;  // the runtime refused it: iterations stay on the host
+                return false;
+            }
+        }
+        const BoundsState& b = ctx->bounds;
+        LoopCtl c{};
+        c.n = n;
+        c.k = k;
+        c.cap = cap;
+        c.cal_select = cal_select;
+        c.bnd = bnd;
+        c.avail = avail;
+        c.kern_extract = (int)g_extract.kernels;
+        for (int v = 0; v < 3; ++v) c.kern_assign[v] = (int)variants[v]->kernels;
+        c.i = i;
+        c.count_iter = countIter;
+        c.sum_class = st.sum_class;
+        c.iterations = cap;
+        c.stop = LOOP_RUN;
+        c.mode = mode;
+        c.old_inertia = old_inertia;
+        c.inertia = st.inertia;
+        c.valid = b.valid;
+        c.refresh = b.refresh;
+        c.regroup = b.regroup;
+        c.passes = b.passes;
+        c.moved = b.moved;
+        c.sum_f = b.sum_f;
+        c.min_f = b.min_f;
+        c.screened = b.screened;
+        c.bounded = b.bounded;
+        c.bounded_pairs = b.bounded_pairs;
+        c.series_pairs = b.series_pairs;
+        TC_CUDA(cudaMemcpyAsync(dctl, &c, sizeof(c), cudaMemcpyHostToDevice, s));
+        TC_CUDA(cudaGraphLaunch(lx.exec, s));
+        TC_CUDA(cudaMemcpyAsync(&c, dctl, sizeof(c), cudaMemcpyDeviceToHost, s));
+        TC_CUDA(cudaMemcpyAsync(&h, aux, sizeof(h), cudaMemcpyDeviceToHost, s));
+        TC_CUDA(cudaStreamSynchronize(s));
+        g_launches.fetch_add(c.launched, std::memory_order_relaxed);
+        ctx->loop.device_iterations += (uint64_t)((c.stop == LOOP_DONE ? c.iterations : c.i) - i);
+        BoundsState& bw = ctx->bounds;
+        bw.valid = c.valid != 0;
+        bw.refresh = c.refresh != 0;
+        bw.regroup = c.regroup != 0;
+        bw.passes = c.passes;
+        bw.moved = c.moved;
+        bw.sum_f = c.sum_f;
+        bw.min_f = c.min_f;
+        bw.screened = c.screened;
+        bw.bounded = c.bounded;
+        bw.bounded_pairs = c.bounded_pairs;
+        bw.series_pairs = c.series_pairs;
+        countIter = c.count_iter;
+        old_inertia = c.old_inertia;
+        st.inertia = c.inertia;
+        st.sum_class = c.sum_class;
+        if (c.stop == LOOP_ERROR) {  // the host's checks, in its order
+            if (h.err[0] || h.err[1]) {
+                ctx->bounds.valid = false;
+                memo_invalidate(ctx);
+            }
+            check_async_errors(h.err);
+            if (h.bad_label) memo_invalidate(ctx);
+            TC_REQUIRE(h.bad_label == 0, TC_ERR_ARG, "a label is outside [0, k)");
+            throw TcError{TC_ERR_CUDA, "the loop graph stopped without a reason"};
+        }
+        if (c.stop == LOOP_DONE) {
+            st.iterations = c.iterations;
+            return true;
+        }
+        i = c.i;
+        return false;
+    };
     for (int i = 0; i < cap; ++i) {
+        if (device_loop(i)) break;
+        ++ctx->loop.host_iterations;
         if (!order_tsl) {
             extract();
             if (st.sum_class == 1 || st.sum_class <= k / 2) {
@@ -492,7 +611,7 @@ static const char* const WS_NAMES[] = {"x", "labels", "old_labels", "shift", "di
                                        "gram", "rowsum", "gram_yt", "gram_poff", "piter", "pstats", "aux",
                                        "toeplitz", "toeplitz_norm", "xbf", "xbf_norm", "first", "gram_sq", "sq_meta", "screen", "gram_part",
                                        "bounds", "cprev", "bstate", "bperm", "xbfp", "tmask", "memo_labels", "memo_c",
-                                       "memo_flags", "memo_count", "fprev"};
+                                       "memo_flags", "memo_count", "fprev", "loopctl"};
 
 static std::vector<DevBuf*> workspace_buffers(tc_ctx* ctx);
 
@@ -530,7 +649,7 @@ static std::vector<DevBuf*> workspace_buffers(tc_ctx* ctx) {
             &w.gram, &w.rowsum,  &w.gram_yt,    &w.gram_poff, &w.piter,   &w.pstats,    &w.aux,
             &w.toeplitz, &w.toeplitz_norm, &w.xbf, &w.xbf_norm, &w.first, &w.gram_sq, &w.sq_meta, &w.screen, &w.gram_part,
             &w.bounds, &w.cprev, &w.bstate, &w.bperm, &w.xbfp, &w.tmask, &w.memo_labels, &w.memo_c,
-            &w.memo_flags, &w.memo_count, &w.fprev};
+            &w.memo_flags, &w.memo_count, &w.fprev, &w.loopctl};
 }
 
 void release_workspace(tc_ctx* ctx) {
@@ -681,6 +800,15 @@ int tc_assign_stats(const tc_ctx* ctx, uint64_t* screened, uint64_t* bounded, ui
     if (screened) *screened = ctx->bounds.screened;
     if (bounded) *bounded = ctx->bounds.bounded;
     if (bounded_pairs) *bounded_pairs = ctx->bounds.bounded_pairs;
+    return TC_OK;
+}
+
+int tc_loop_stats(const tc_ctx* ctx, uint64_t* device_iterations, uint64_t* host_iterations,
+                  uint64_t* graphs_built) {
+    if (!ctx) return TC_ERR_ARG;
+    if (device_iterations) *device_iterations = ctx->loop.device_iterations;
+    if (host_iterations) *host_iterations = ctx->loop.host_iterations;
+    if (graphs_built) *graphs_built = ctx->loop.builds;
     return TC_OK;
 }
 

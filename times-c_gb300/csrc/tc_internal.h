@@ -154,6 +154,7 @@ struct Workspace {
     DevBuf memo_c;       // 3 x k x m f32: that extraction's input and output centroids, this one's input
     DevBuf memo_flags;   // 3k u8 (dirty, skip, gate for the shift pass) + an i32 valid word
     DevBuf memo_count;   // 3 u64: extractions with the memo, clusters they covered, clusters skipped
+    DevBuf loopctl;      // the loop graph's state (LoopCtl)
 };
 
 // The extraction's memo (extract.cu): the key of the previous extraction whose
@@ -206,6 +207,11 @@ struct tc_ctx {
     BoundsState bounds;
     // memo of unchanged clusters in the extraction (same series: prepared, or the run's own)
     MemoState memo;
+    // iterations of tc_kshape_run run by the loop graph and by the host, graphs built
+    struct {
+        uint64_t device_iterations = 0, host_iterations = 0, builds = 0;
+    } loop;
+    bool loop_graph_failed = false;  // the runtime refused a loop graph: the host runs iterations
 };
 
 namespace tc {

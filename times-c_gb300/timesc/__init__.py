@@ -66,6 +66,8 @@ SIGNATURES = {
                                ctypes.POINTER(ctypes.c_uint64)]),
     "tc_extract_stats": (_int, [_vp, ctypes.POINTER(ctypes.c_uint64), ctypes.POINTER(ctypes.c_uint64),
                                 ctypes.POINTER(ctypes.c_uint64)]),
+    "tc_loop_stats": (_int, [_vp, ctypes.POINTER(ctypes.c_uint64), ctypes.POINTER(ctypes.c_uint64),
+                             ctypes.POINTER(ctypes.c_uint64)]),
     "tc_sbd_assign_noalloc": (_int, [_vp, _vp, _i64, _int, _int, _int, _vp, _vp, _vp, ctypes.c_char_p, _int]),
     "tc_extract_shapes": (_int, [_vp, _vp, _vp, _vp, _vp, _i64, _int, _int, _int, _int, _int, _vp,
                                  ctypes.POINTER(_int), _vp]),
@@ -182,6 +184,13 @@ class Context:
         reused unchanged (synchronises the device)."""
         a, b, c = ctypes.c_uint64(), ctypes.c_uint64(), ctypes.c_uint64()
         self._check(lib().tc_extract_stats(self.h, ctypes.byref(a), ctypes.byref(b), ctypes.byref(c)))
+        return a.value, b.value, c.value
+
+    def loop_stats(self):
+        """(device_iterations, host_iterations, graphs_built): kshape_run iterations on
+        this context that ran inside the loop graph and on the host, and loop graphs built."""
+        a, b, c = ctypes.c_uint64(), ctypes.c_uint64(), ctypes.c_uint64()
+        self._check(lib().tc_loop_stats(self.h, ctypes.byref(a), ctypes.byref(b), ctypes.byref(c)))
         return a.value, b.value, c.value
 
     def prepare_series(self, x, stream=None):
