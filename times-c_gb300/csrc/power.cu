@@ -481,7 +481,16 @@ void power_eigvecs(tc_ctx* ctx, const float* S, int ld, const double* r, const d
         const bool hold = (m + 7) / 8 <= (PC_THREADS / 32) * PC_UNROLL && nv4 <= 128;
         const bool res = cluster_smem<8>(m, ld, true) + 4096 <= ctx->smem_optin && !std::getenv("TIMESC_POWER_L2");
         const size_t smem = cluster_smem<8>(m, ld, res && !hold);
-        if (hold) {
+        // with rows in registers, the smallest cluster whose CTAs hold them (64 rows a
+        // CTA): a step's exchange and cluster barrier then span fewer CTAs
+        constexpr int HOLD_ROWS = (PC_THREADS / 32) * PC_UNROLL;
+        if (hold && m <= HOLD_ROWS && nv4 <= 32) {
+            launch_cluster<1, 1, false, true>(pp, k, cluster_smem<1>(m, ld, false), s);
+        } else if (hold && m <= 2 * HOLD_ROWS && nv4 <= 32) {
+            launch_cluster<2, 1, false, true>(pp, k, cluster_smem<2>(m, ld, false), s);
+        } else if (hold && m <= 4 * HOLD_ROWS && nv4 <= 64) {
+            launch_cluster<4, 2, false, true>(pp, k, cluster_smem<4>(m, ld, false), s);
+        } else if (hold) {
             if (nv4 <= 32) launch_cluster<8, 1, false, true>(pp, k, smem, s);
             else if (nv4 <= 64) launch_cluster<8, 2, false, true>(pp, k, smem, s);
             else launch_cluster<8, 4, false, true>(pp, k, smem, s);
