@@ -106,7 +106,9 @@ def _loop(exe, tmp, log, x, k, init_chose, cap, seed):
 
 
 def main():
-    out_dir = sys.argv[1] if len(sys.argv) > 1 else os.path.join(ROOT, "gpurun_out")
+    if len(sys.argv) < 2 or sys.argv[1].startswith("-"):
+        sys.exit("usage: make_ref_gpu_golden.py OUT_DIR [--time]")
+    out_dir = sys.argv[1]
     os.makedirs(out_dir, exist_ok=True)
     exe = _ref_gpu()
     import timesc

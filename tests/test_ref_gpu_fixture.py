@@ -97,7 +97,7 @@ def test_oracle_loop_matches_reference_gpu(built, gold, name, init_chose, seed):
 def test_reference_not_reproducible_above_1024(built):
     """At m = 2709 the reference's norm_vec rescales each power-iteration vector from
     three 1024-thread blocks while the others still read it (shapeExtract.cuh:
-    287-323, SURVEY's inter-block race): two runs of its extraction on the same
+    287-323: a race between thread blocks): two runs of its extraction on the same
     input disagree, and so do two runs of its whole init_chose=0 loop."""
     g = np.load(GOLDEN_C2)
     a, b = g["extract_zero_cal0_run0"], g["extract_zero_cal0_run1"]
