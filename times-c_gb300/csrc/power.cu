@@ -89,7 +89,12 @@ __global__ void __launch_bounds__(PC_THREADS, 1) k_power_cluster(PowerClusterPar
     cg::cluster_group cluster = cg::this_cluster();
     extern __shared__ __align__(16) unsigned char dsm[];
     const int m = p.m, ld = p.ld;
-    const int rank = (int)cluster.block_rank();
+    const int rank = CL == 1 ? 0 : (int)cluster.block_rank();
+    // one CTA per k-Shape cluster: plain shared memory and CTA barriers
+    auto cluster_sync = [&]() {
+        if constexpr (CL == 1) __syncthreads();
+        else cluster.sync();
+    };
     const int c = blockIdx.x / CL;
     if (p.counts[c] == 0 || (p.skip && p.skip[c])) return;  // every CTA of this cluster leaves together
     const int a0 = (int)((int64_t)rank * m / CL), a1 = (int)((int64_t)(rank + 1) * m / CL);
@@ -175,8 +180,8 @@ __global__ void __launch_bounds__(PC_THREADS, 1) k_power_cluster(PowerClusterPar
         __syncthreads();
     }
     // lane q < CL stores into CTA q: one remote address per lane
-    float* yre = cluster.map_shared_rank(ybuf, lane < CL ? lane : 0);
-    float2* pre = cluster.map_shared_rank(part, lane < CL ? lane : 0);
+    float* yre = CL == 1 ? ybuf : cluster.map_shared_rank(ybuf, lane < CL ? lane : 0);
+    float2* pre = CL == 1 ? part : cluster.map_shared_rank(part, lane < CL ? lane : 0);
     constexpr int U = BPL >= 8 ? 2 : PC_UNROLL;  // rows in flight per warp
     constexpr int XU = HOLD ? U : 1, XB = HOLD ? BPL : 1;
     float4 xh[XU][XB];  // HOLD: this warp's rows wid*U.., loaded once
@@ -191,7 +196,7 @@ __global__ void __launch_bounds__(PC_THREADS, 1) k_power_cluster(PowerClusterPar
                                : make_float4(0.f, 0.f, 0.f, 0.f);
             }
     }
-    cluster.sync();  // every CTA initialised before remote stores start
+    cluster_sync();  // every CTA initialised before remote stores start
     int T = tmax;
     float fsc = 1.f;  // v_t = ybuf[(t-1)&1] * fsc for t >= 1 (the FP32 product the update stored before)
     for (int t = 0;; ++t) {
@@ -314,7 +319,7 @@ __global__ void __launch_bounds__(PC_THREADS, 1) k_power_cluster(PowerClusterPar
 #pragma unroll
             for (int q = 0; q < 4; ++q) dst[q] = mine[q];
         }
-        cluster.sync();  // y and partials of step t visible in every CTA
+        cluster_sync();  // y and partials of step t visible in every CTA
         if (wid == 0) {  // the same fixed order in every CTA, so all take the same decision
             float ts[4] = {0.f, 0.f, 0.f, 0.f}, tcm[4] = {0.f, 0.f, 0.f, 0.f};
             const float2* pp = part + (size_t)par * CL * NWARP * 4;
@@ -426,7 +431,7 @@ __global__ void __launch_bounds__(PC_THREADS, 1) k_power_cluster(PowerClusterPar
         }
         if (threadIdx.x == 0 && p.steps) p.steps[c] = T;
     }
-    cluster.sync();  // no CTA leaves while another may still touch its shared memory
+    cluster_sync();  // no CTA leaves while another may still touch its shared memory
 }
 
 // ---------------------------------------------------------------- host
