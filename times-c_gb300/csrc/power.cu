@@ -280,6 +280,10 @@ __global__ void __launch_bounds__(PC_THREADS, 1) k_power_cluster(PowerClusterPar
                     for (int u = 0; u < U; ++u) kahan4(u, x[u], w);
                 }
             }
+            // a warp's U = 4 rows are consecutive: one 16-byte store per CTA instead of
+            // four (the remote stores of a step are what its cluster barrier waits for)
+            float yq[U];
+            const bool vec4 = U == 4 && (a0 & 3) == 0 && i0 + U <= nrow;
 #pragma unroll
             for (int u = 0; u < U; ++u) {
 #pragma unroll
@@ -293,7 +297,9 @@ __global__ void __launch_bounds__(PC_THREADS, 1) k_power_cluster(PowerClusterPar
                     const int a = a0 + i;
                     const float ra = r_own[i];
                     const float yf = (s[u] - cp[u]) + fmaf(cr, ra, cc);
-                    if (lane < CL) yre[par * ld + a] = yf;  // into every CTA of the cluster
+                    yq[u] = yf;
+                    // into every CTA of the cluster (four rows at once below when they can)
+                    if (lane < CL && !vec4) yre[par * ld + a] = yf;
                     if (lane == 0) {
                         add_prod(0, yf, yf);
                         two_sum_acc(accs[1], accc[1], yf, 0.f);
@@ -307,6 +313,10 @@ __global__ void __launch_bounds__(PC_THREADS, 1) k_power_cluster(PowerClusterPar
                     }
                 }
             }
+            if constexpr (U == 4) {
+                if (vec4 && lane < CL)
+                    *reinterpret_cast<float4*>(yre + par * ld + a0 + i0) = make_float4(yq[0], yq[1], yq[2], yq[3]);
+            }
         }
         // every warp's partial (held by lane 0) straight into every CTA, lane q storing into
         // CTA q: no CTA barrier before the exchange
@@ -314,10 +324,10 @@ __global__ void __launch_bounds__(PC_THREADS, 1) k_power_cluster(PowerClusterPar
 #pragma unroll
         for (int q = 0; q < 4; ++q)
             mine[q] = make_float2(__shfl_sync(0xffffffffu, accs[q], 0), __shfl_sync(0xffffffffu, accc[q], 0));
-        if (lane < CL) {
-            float2* dst = pre + ((size_t)(par * CL + rank) * NWARP + wid) * 4;
-#pragma unroll
-            for (int q = 0; q < 4; ++q) dst[q] = mine[q];
+        if (lane < CL) {  // 32 bytes at a 32-byte offset: two 16-byte stores
+            float4* dst = reinterpret_cast<float4*>(pre + ((size_t)(par * CL + rank) * NWARP + wid) * 4);
+            dst[0] = make_float4(mine[0].x, mine[0].y, mine[1].x, mine[1].y);
+            dst[1] = make_float4(mine[2].x, mine[2].y, mine[3].x, mine[3].y);
         }
         cluster_sync();  // y and partials of step t visible in every CTA
         if (wid == 0) {  // the same fixed order in every CTA, so all take the same decision
