@@ -124,8 +124,9 @@ int tc_prepare_series(tc_ctx* ctx, const float* d_x, int64_t n, int m, tc_stream
  * would have.  screened: calls that built
  * bounds; bounded: calls that used them; bounded_pairs: pairs those evaluated (out
  * of n*k each, counted in whole 128-series tiles).  Any output may be NULL.
- * TIMESC_NO_BOUNDS=1 in the environment turns the bounds off.  No counterpart in
- * the reference. */
+ * TIMESC_NO_BOUNDS=1 in the environment turns the bounds off; TIMESC_REGROUP_SHARE=s
+ * groups the series anew once 1/s of them changed best centroid (default 20).  No
+ * counterpart in the reference. */
 int tc_assign_stats(const tc_ctx* ctx, uint64_t* screened, uint64_t* bounded, uint64_t* bounded_pairs);
 
 /* Work the extraction memo saved on this context since its creation: extractions

@@ -61,6 +61,26 @@ def test_loop_with_bounds_equals_dense(built, prec, mode, n, m, k, init_chose):
 
 
 @pytest.mark.parametrize("prec", [0, 1])
+def test_loop_regrouping_every_pass_equals_dense(built, prec):
+    """TIMESC_REGROUP_SHARE=1000000: every bounded pass after a moved series first
+    groups the series anew (the path the default threshold takes less often)."""
+    T, _ = built
+    n, m, k = 8000, 256, 16
+    data, _ = T.generate(n, m, k, noise=0.3, seed=17)
+    ctx = T.Context(0)
+    os.environ["TIMESC_REGROUP_SHARE"] = "1000000"
+    try:
+        a = _run(ctx, data, k, 0, 0, 3, bounds=True, prec=prec)
+        b = _run(ctx, data, k, 0, 0, 3, bounds=False, prec=prec)
+    finally:
+        os.environ.pop("TIMESC_REGROUP_SHARE", None)
+        ctx.close()
+    assert a["iterations"] == b["iterations"] >= 3
+    assert np.array_equal(a["labels"], b["labels"])
+    assert np.array_equal(a["centroids"], b["centroids"])
+
+
+@pytest.mark.parametrize("prec", [0, 1])
 def test_stage_calls_with_bounds_ties_zero_and_flip(built, prec):
     """Stage calls on prepared series: each call with bounds against a context that
     evaluates every pair, over a sequence of centroid sets with small moves, an exact

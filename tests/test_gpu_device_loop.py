@@ -75,6 +75,19 @@ def test_loop_graph_equals_host_loop(built, mode, prec, n, m, k, init_chose, max
         assert d_it >= 1 and builds >= 1
 
 
+def test_loop_graph_regrouping_every_pass(built):
+    """The loop graph's control kernel takes the regroup threshold it was given."""
+    T, _ = built
+    data, _ = T.generate(8000, 256, 16, noise=0.3, seed=17)
+    os.environ["TIMESC_REGROUP_SHARE"] = "1000000"
+    try:
+        host = _run(T, data, 16, False, precision=1, seed=3, max_iter=25)
+        dev = _run(T, data, 16, True, precision=1, seed=3, max_iter=25)
+    finally:
+        os.environ.pop("TIMESC_REGROUP_SHARE", None)
+    _same(host, dev)
+
+
 def test_loop_graph_with_restart(built):
     T, _ = built
     data, _ = T.generate(300, 128, 4, noise=0.3, seed=0)

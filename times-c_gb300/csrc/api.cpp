@@ -62,7 +62,7 @@ static void check_shape(int64_t n, int m, int k, int mode) {
 //     groups the series by best and second-best centroid.
 //   * A bounded pass (BOUNDS_USE) evaluates the tiles' masks; BOUNDS_USE_REGROUP first
 //     groups the series anew by the keys the previous pass left, which the next pass
-//     does once more than 1/200 of the series changed their best centroid since the
+//     does once more than 1/20 of the series changed their best centroid since the
 //     last grouping (a moved series widens its old tile's mask).
 //   * Every evaluated pair gets a fresh bound, so only the skipped ones loosen; a full
 //     pass is run again once the bounded passes since the last one have cost, beyond
@@ -72,6 +72,13 @@ static void check_shape(int64_t n, int m, int k, int mode) {
 // the same rule on the device.)
 
 static bool bounded_mode(int use) { return use == BOUNDS_USE || use == BOUNDS_USE_REGROUP; }
+
+// The regroup threshold's denominator (BOUNDS_REGROUP_SHARE, or TIMESC_REGROUP_SHARE).
+static int64_t regroup_share() {
+    const char* e = std::getenv("TIMESC_REGROUP_SHARE");
+    const long long v = e ? std::atoll(e) : 0;
+    return v > 0 ? (int64_t)v : BOUNDS_REGROUP_SHARE;
+}
 
 // Bounds are kept for the FP32 form where the screened pass runs, and for the BF16
 // form where the tensor-core correlation runs with k <= 64 (one mask word per tile).
@@ -255,7 +262,7 @@ static void bounds_feedback(tc_ctx* ctx, int used, unsigned long long evals, uns
                          used == BOUNDS_USE_REGROUP ? " (regrouped)" : "", (double)evals / ((double)n * k),
                          (double)spairs / ((double)n * k));
         b.moved = (used == BOUNDS_USE_REGROUP ? 0 : b.moved) + moved;
-        b.regroup = (int64_t)b.moved * BOUNDS_REGROUP_SHARE > n;
+        b.regroup = (int64_t)b.moved * regroup_share() > n;
         const double f = (double)evals / ((double)n * k);
         b.sum_f += f;
         b.min_f = std::min(b.min_f, f);
@@ -518,6 +525,7 @@ static LoopState run_loop(tc_ctx* ctx, const tc_job* job, const float* x, int k,
         const BoundsState& b = ctx->bounds;
         LoopCtl c{};
         c.n = n;
+        c.regroup_share = regroup_share();
         c.k = k;
         c.cap = cap;
         c.cal_select = cal_select;

@@ -60,7 +60,7 @@ __device__ void bounds_feedback(LoopCtl& c, int used, unsigned long long evals, 
         c.bounded_pairs += evals;
         c.series_pairs += spairs;
         c.moved = (used == BOUNDS_USE_REGROUP ? 0ull : c.moved) + moved;
-        c.regroup = (long long)c.moved * BOUNDS_REGROUP_SHARE > c.n;
+        c.regroup = (long long)c.moved * c.regroup_share > c.n;
         const double f = __ddiv_rn((double)evals, __dmul_rn((double)c.n, (double)c.k));
         c.sum_f = __dadd_rn(c.sum_f, f);
         c.min_f = f < c.min_f ? f : c.min_f;

@@ -26,8 +26,11 @@ enum { BOUNDS_OFF = 0, BOUNDS_AUTO = -1, BOUNDS_REFRESH = 1, BOUNDS_USE = 2, BOU
 // a full pass again once the bounded passes since the last one cost, beyond the
 // cheapest of them, one full pass (sum of evaluated fractions - passes x minimum)
 constexpr double BOUNDS_REFRESH_COST = 1.0;
-// regroup once more than 1/200 of the series changed best centroid since the last grouping
-constexpr int64_t BOUNDS_REGROUP_SHARE = 200;
+// regroup once more than 1/20 of the series changed best centroid since the last grouping
+// (at n = 1e6, m = 512, k = 32: 6.15 ms per iteration against 6.21 at 1/200 and 6.16
+// with no regrouping, whose first bounded passes evaluate up to 15% more pairs)
+// (TIMESC_REGROUP_SHARE=s in the environment: 1/s)
+constexpr int64_t BOUNDS_REGROUP_SHARE = 20;
 
 // The assignment stage variants a loop graph holds: 0 full pass (or no bounds),
 // 1 bounded pass, 2 bounded pass on a new grouping.
@@ -41,6 +44,7 @@ enum { LOOP_RUN = 0, LOOP_DONE = 1, LOOP_ERROR = 2, LOOP_HOST = 3 };
 struct LoopCtl {
     // fixed for the launch
     int64_t n;
+    int64_t regroup_share;  // regroup once moved x regroup_share > n
     int k, cap, cal_select, bnd;
     int avail;           // bit v: assignment variant v is in the graph
     int kern_extract;    // kernels of one extraction stage
