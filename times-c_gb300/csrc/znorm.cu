@@ -10,6 +10,8 @@
 // (block_alloc2D + sbd3D + z_norm_gpu_x of shapeExtract.cuh:1117-1141).
 #include <cuda_bf16.h>
 
+#include <type_traits>
+
 #include "tc_internal.h"
 
 namespace tc {
@@ -244,23 +246,48 @@ __global__ void __launch_bounds__(256) k_gather_norm_t(const float* __restrict__
         const float* x = src + (size_t)i * m;
         const int sh = (gate && shift && gate[c]) ? shift[i] : 0;
         float v[VPL];
-        KSum s;
 #pragma unroll
         for (int q = 0; q < VPL; ++q) {
             const int t = lane + 32 * q, a = t - sh;
             v[q] = (t < m && a >= 0 && a < m) ? x[a] : 0.f;
-            s.add(v[q]);
         }
-        const float mean = warp_sum_comp(s) / (float)m;
-        KSum ss;
+        float mean, var;
+        if constexpr (std::is_same<TO, float>::value) {
+            // FP32 operand (its 3xTF32 low plane keeps FP32 accuracy): compensated sums
+            KSum s;
 #pragma unroll
-        for (int q = 0; q < VPL; ++q) {
-            const int t = lane + 32 * q;
-            const float d = t < m ? v[q] - mean : 0.f;
-            v[q] = d;
-            ss.add(d * d);
+            for (int q = 0; q < VPL; ++q) s.add(v[q]);
+            mean = warp_sum_comp(s) / (float)m;
+            KSum ss;
+#pragma unroll
+            for (int q = 0; q < VPL; ++q) {
+                const int t = lane + 32 * q;
+                const float d = t < m ? v[q] - mean : 0.f;
+                v[q] = d;
+                ss.add(d * d);
+            }
+            var = warp_sum_comp(ss) / (float)(m - 1);
+        } else {
+            // BF16 operand: plain FP32 sums (relative error ~1e-5 in the scale, far below
+            // BF16's 4e-3 rounding step), a third of the compensated form's instructions
+            float s = 0.f;
+#pragma unroll
+            for (int q = 0; q < VPL; ++q) s += v[q];
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+            mean = s / (float)m;
+            float ss = 0.f;
+#pragma unroll
+            for (int q = 0; q < VPL; ++q) {
+                const int t = lane + 32 * q;
+                const float d = t < m ? v[q] - mean : 0.f;
+                v[q] = d;
+                ss = fmaf(d, d, ss);
+            }
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) ss += __shfl_xor_sync(0xffffffffu, ss, o);
+            var = ss / (float)(m - 1);
         }
-        const float var = warp_sum_comp(ss) / (float)(m - 1);
         const float sd = sqrtf(var);
         const float inv = (sd > 0.f && isfinite(sd)) ? 1.0f / sd : 0.f;
         const bool lead = pos == offsets[c];
